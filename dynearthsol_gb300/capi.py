@@ -1,0 +1,249 @@
+"""ctypes mirror of ``include/desgpu.h`` and loader of the CUDA library.
+
+The structs below are byte-for-byte the C structs of the header; the loader
+finds ``libdesgpu.so`` next to this file (built in-tree by
+``dynearthsol_gb300.build``) and raises when it is missing, so no caller can
+silently run without the CUDA path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+NBDRY = 10
+
+DES_OK = 0
+DES_EINPUT = 1
+DES_ECUDA = 3
+DES_ENOMEM = 4
+DES_ERUNTIME = 11
+DES_EASSERT = 12
+
+DES_DEV_NONFINITE = 1
+DES_DEV_NEG_VOLUME = 2
+DES_DEV_QL_NOCONV = 4
+DES_DEV_BAD_INDEX = 8
+
+RH_ELASTIC = 1
+RH_VISCOUS = 2
+RH_PLASTIC = 4
+RH_MAXWELL = RH_ELASTIC | RH_VISCOUS
+RH_EP = RH_ELASTIC | RH_PLASTIC
+RH_EVP = RH_ELASTIC | RH_VISCOUS | RH_PLASTIC
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+EF_COHESION0 = 0
+EF_COHESION1 = 1
+EF_LOG10_VISC = 2
+EF_SHEAR_MODULUS = 3
+EF_FRICTION0 = 4
+EF_FRICTION1 = 5
+EF_THERM_COND = 6
+EF_COUNT = 7
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_up = C.POINTER(C.c_uint)
+
+
+class DesMesh(C.Structure):
+    _fields_ = [
+        ("ndims", C.c_int),
+        ("nnode", C.c_int),
+        ("nelem", C.c_int),
+        ("connectivity", _ip),
+        ("bcflag", _up),
+        ("bfacet_offsets", _ip),
+        ("bfacets", _ip),
+        ("bnormals", (C.c_double * 3) * NBDRY),
+        ("edge_vectors", ((C.c_double * 3) * NBDRY) * NBDRY),
+    ]
+
+
+class DesParams(C.Structure):
+    _fields_ = [
+        ("gravity", C.c_double),
+        ("inertial_scaling", C.c_double),
+        ("dt_fraction", C.c_double),
+        ("fixed_dt", C.c_double),
+        ("damping_factor", C.c_double),
+        ("surface_diffusivity", C.c_double),
+        ("max_vbc_val", C.c_double),
+        ("damping_option", C.c_int),
+        ("ref_pressure_option", C.c_int),
+        ("surface_process_option", C.c_int),
+        ("is_quasi_static", C.c_int),
+        ("has_thermal_diffusion", C.c_int),
+        ("surface_temperature", C.c_double),
+        ("mantle_temperature", C.c_double),
+        ("winkler_delta_rho", C.c_double),
+        ("elastic_foundation_constant", C.c_double),
+        ("has_fixed_bottom_temperature", C.c_int),
+        ("has_winkler_foundation", C.c_int),
+        ("has_elastic_foundation", C.c_int),
+        ("has_water_loading", C.c_int),
+        ("vbc_types", C.c_int * NBDRY),
+        ("vbc_values", C.c_double * NBDRY),
+        ("zlength", C.c_double),
+        ("compensation_pressure", C.c_double),
+    ]
+
+
+MAT_ARRAYS = (
+    "rho0", "alpha", "bulk_modulus", "shear_modulus", "visc_exponent",
+    "visc_coefficient", "visc_activation_energy", "heat_capacity", "therm_cond",
+    "radiogenic_heating", "pls0", "pls1", "cohesion0", "cohesion1",
+    "friction_angle0", "friction_angle1", "dilation_angle0", "dilation_angle1",
+)
+
+
+class DesMaterial(C.Structure):
+    _fields_ = [
+        ("rheol_type", C.c_int),
+        ("nmat", C.c_int),
+        ("is_plane_strain", C.c_int),
+        ("scalar_mask", C.c_uint),
+        ("visc_min", C.c_double),
+        ("visc_max", C.c_double),
+        ("tension_max", C.c_double),
+        ("therm_diff_max", C.c_double),
+    ] + [(name, _dp) for name in MAT_ARRAYS] + [("elemmarkers", _ip)]
+
+
+STATE_ARRAYS = (
+    "coord", "coord0", "vel", "force", "temperature", "mass", "tmass", "volume_n",
+    "ntmp", "volume", "volume_old", "stress", "strain", "strain_rate", "plstrain",
+    "delta_plstrain", "stressyy", "dpressure", "edvoldt", "shpdx", "shpdy", "shpdz",
+)
+
+
+class DesHostState(C.Structure):
+    _fields_ = [(name, _dp) for name in STATE_ARRAYS] + [
+        ("time", C.c_double),
+        ("dt", C.c_double),
+        ("steps", C.c_int),
+    ]
+
+
+def dptr(a: np.ndarray | None):
+    """double* of a C-contiguous float64 array (NULL for None)."""
+    if a is None:
+        return _dp()
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a: np.ndarray | None):
+    if a is None:
+        return _ip()
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ip)
+
+
+def uptr(a: np.ndarray | None):
+    if a is None:
+        return _up()
+    assert a.dtype == np.uint32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_up)
+
+
+# --------------------------------------------------------------------------
+# CUDA library
+# --------------------------------------------------------------------------
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdesgpu.so")
+
+_lib = None
+
+# (name, argtypes); every entry point returns int
+_SIGS = {
+    "des_create": [C.POINTER(DesMesh), C.POINTER(DesParams), C.POINTER(DesMaterial), C.c_int,
+                   C.c_void_p, C.POINTER(C.c_void_p)],
+    "des_destroy": [C.c_void_p],
+    "des_last_error": [C.c_void_p, C.c_char_p, C.c_size_t],
+    "des_device_status": [C.c_void_p, _up],
+    "des_upload_state": [C.c_void_p, C.POINTER(DesHostState)],
+    "des_download_state": [C.c_void_p, C.POINTER(DesHostState)],
+    "des_set_params": [C.c_void_p, C.POINTER(DesParams)],
+    "des_set_elem_field": [C.c_void_p, C.c_int, _dp],
+    "des_update_temperature": [C.c_void_p],
+    "des_update_strain_rate": [C.c_void_p],
+    "des_compute_dvoldt": [C.c_void_p],
+    "des_compute_edvoldt": [C.c_void_p],
+    "des_update_stress": [C.c_void_p],
+    "des_NMD_stress": [C.c_void_p],
+    "des_update_force": [C.c_void_p],
+    "des_update_velocity": [C.c_void_p],
+    "des_apply_vbcs": [C.c_void_p],
+    "des_update_coordinate": [C.c_void_p],
+    "des_swap_volume": [C.c_void_p],
+    "des_compute_volume": [C.c_void_p],
+    "des_compute_mass": [C.c_void_p],
+    "des_compute_shape_fn": [C.c_void_p],
+    "des_rotate_stress": [C.c_void_p],
+    "des_compute_dt": [C.c_void_p, _dp],
+    "des_update_mesh": [C.c_void_p],
+    "des_worst_elem_quality": [C.c_void_p, _dp, _ip],
+    "des_get_clock": [C.c_void_p, _dp, _dp, _ip],
+    "des_set_clock": [C.c_void_p, C.c_double, C.c_double, C.c_int],
+    "des_step": [C.c_void_p, C.c_int],
+    "des_step_host": [C.c_void_p, C.POINTER(DesHostState), C.c_int],
+    "des_synchronize": [C.c_void_p],
+    "des_launch_count": [C.c_void_p, C.POINTER(C.c_longlong)],
+}
+
+
+def declared_symbols() -> list[str]:
+    """Entry points declared in include/desgpu.h (parsed from the header)."""
+    import re
+
+    hdr = os.path.join(os.path.dirname(HERE), "include", "desgpu.h")
+    text = open(hdr).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(des_\w+)\s*\(", text, re.M)))
+
+
+def load_library(path: str | None = None):
+    """Load libdesgpu.so (raises OSError when it was not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"libdesgpu.so not found at {p}; build it with "
+                      "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(p)
+    for name, args in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.des_version.argtypes = []
+    lib.des_version.restype = C.c_char_p
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class DesError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"desgpu error {code}: {msg}")
+        self.code = code
+
+
+def host_state_struct(st: dict, time: float = 0.0, dt: float = 0.0, steps: int = 0) -> DesHostState:
+    """DesHostState pointing into the float64 arrays of a state dict (keys of
+    STATE_ARRAYS; missing keys become NULL).  The dict must outlive it."""
+    s = DesHostState()
+    for name in STATE_ARRAYS:
+        a = st.get(name)
+        if a is not None:
+            if a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError(f"state array {name} must be C-contiguous float64")
+            setattr(s, name, dptr(a))
+    s.time = time
+    s.dt = dt
+    s.steps = steps
+    return s

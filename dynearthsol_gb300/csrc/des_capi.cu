@@ -1,0 +1,760 @@
+// des_capi.cu -- C ABI of the explicit-step library (include/desgpu.h):
+// context creation (topology products on the host, one device pool),
+// host <-> device state transfer in the reference's layout, the
+// per-function entry points and the CUDA-graph-replayed fused step.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "des_kernels.cuh"
+
+using namespace des;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail_msg(std::string &dst, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    dst = buf;
+    return code;
+}
+
+}  // namespace
+
+struct des_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int precision = DES_PREC_FP64;
+    int nd = 0, npe = 0, nstr = 0, nn = 0, ne = 0, nbf = 0;
+    KP kp{};                      // per-function parameter block (no step scratch)
+    char *pool = nullptr;         // one device allocation for every array
+    size_t pool_bytes = 0;
+    double *d_tdot = nullptr;     // node scratch of the fused step
+    double *d_rho = nullptr;      // element scratch of the fused step
+    double *d_stage = nullptr;    // AoS staging buffer
+    size_t stage_doubles = 0;
+    unsigned long long *d_red = nullptr;
+    double *d_ef[DES_EF_COUNT] = {};
+    cudaGraphExec_t step_exec = nullptr;
+    int step_kernels = 0;
+    long long launches = 0;
+    std::string err;
+    bool has_state = false;
+};
+
+namespace {
+
+int cuda_fail(des_ctx *c, cudaError_t e, const char *what)
+{
+    std::string &dst = c ? c->err : g_create_error;
+    return fail_msg(dst, DES_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call)                                        \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+    } while (0)
+
+int check_launch(des_ctx *c, int n)
+{
+    c->launches += n;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, "kernel launch");
+    return DES_OK;
+}
+
+KP step_kp(const des_ctx *c)
+{
+    KP p = c->kp;
+    p.rho_e = c->d_rho;
+    p.tdot = c->d_tdot;
+    return p;
+}
+
+void invalidate_graph(des_ctx *c)
+{
+    if (c->step_exec) {
+        cudaGraphExecDestroy(c->step_exec);
+        c->step_exec = nullptr;
+    }
+}
+
+int set_params(des_ctx *c, const des_params *prm)
+{
+    if (prm->ref_pressure_option != 0)
+        return fail_msg(c->err, DES_EINPUT, "ref_pressure_option %d is not supported on the device (only 0)",
+                        prm->ref_pressure_option);
+    if (prm->surface_process_option != 0)
+        return fail_msg(c->err, DES_EINPUT,
+                        "surface_process_option %d runs on the host; the device step supports 0",
+                        prm->surface_process_option);
+    if (prm->damping_option < 0 || prm->damping_option > 4)
+        return fail_msg(c->err, DES_EINPUT, "unknown damping_option: %d", prm->damping_option);
+    c->kp.prm = *prm;
+    invalidate_graph(c);
+    return DES_OK;
+}
+
+int set_material(des_ctx *c, const des_material *m)
+{
+    MatC &t = c->kp.mat;
+    const int rt = m->rheol_type;
+    if (rt != DES_RH_ELASTIC && rt != DES_RH_VISCOUS && rt != DES_RH_MAXWELL && rt != DES_RH_EP &&
+        rt != DES_RH_EVP)
+        return fail_msg(c->err, DES_EINPUT, "unknown rheology type: %d", rt);
+    if (m->nmat < 1 || m->nmat > DES_MAXMAT)
+        return fail_msg(c->err, DES_EINPUT, "nmat = %d outside 1..%d", m->nmat, DES_MAXMAT);
+    t.rheol_type = rt;
+    t.nmat = m->nmat;
+    t.is_plane_strain = m->is_plane_strain;
+    t.scalar_mask = m->scalar_mask;
+    t.visc_min = m->visc_min;
+    t.visc_max = m->visc_max;
+    t.tension_max = m->tension_max;
+    t.therm_diff_max = m->therm_diff_max;
+    const double *src[] = {m->rho0, m->alpha, m->bulk_modulus, m->shear_modulus, m->visc_exponent,
+                           m->visc_coefficient, m->visc_activation_energy, m->heat_capacity, m->therm_cond,
+                           m->radiogenic_heating, m->pls0, m->pls1, m->cohesion0, m->cohesion1,
+                           m->friction_angle0, m->friction_angle1, m->dilation_angle0, m->dilation_angle1};
+    double *dst[] = {t.rho0, t.alpha, t.bulk_modulus, t.shear_modulus, t.visc_exponent, t.visc_coefficient,
+                     t.visc_activation_energy, t.heat_capacity, t.therm_cond, t.radiogenic_heating, t.pls0,
+                     t.pls1, t.cohesion0, t.cohesion1, t.friction_angle0, t.friction_angle1,
+                     t.dilation_angle0, t.dilation_angle1};
+    for (int k = 0; k < 18; ++k) {
+        if (!src[k]) return fail_msg(c->err, DES_EINPUT, "material array %d is NULL", k);
+        for (int i = 0; i < m->nmat; ++i) dst[k][i] = src[k][i];
+    }
+    return DES_OK;
+}
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" {
+
+const char *des_version(void) { return "desgpu 0.1 (sm_103a, FP64 explicit step)"; }
+
+int des_last_error(const des_ctx *c, char *buf, size_t len)
+{
+    if (!buf || len == 0) return DES_EINPUT;
+    const std::string &s = c ? c->err : g_create_error;
+    size_t n = std::min(len - 1, s.size());
+    memcpy(buf, s.data(), n);
+    buf[n] = 0;
+    return DES_OK;
+}
+
+int des_create(const des_mesh *mesh, const des_params *param, const des_material *mat, int precision,
+               void *stream, des_ctx **out)
+{
+    des_ctx *c = nullptr;
+    if (!out) return fail_msg(g_create_error, DES_EINPUT, "out is NULL");
+    *out = nullptr;
+    if (!mesh || !param || !mat) return fail_msg(g_create_error, DES_EINPUT, "NULL mesh/param/material");
+    if (mesh->ndims != 2 && mesh->ndims != 3)
+        return fail_msg(g_create_error, DES_EINPUT, "ndims must be 2 or 3 (got %d)", mesh->ndims);
+    if (mesh->nnode <= 0 || mesh->nelem <= 0)
+        return fail_msg(g_create_error, DES_EINPUT, "empty mesh (nnode=%d, nelem=%d)", mesh->nnode, mesh->nelem);
+    if ((long long)mesh->nelem * 4 >= (1ll << 31))
+        return fail_msg(g_create_error, DES_EINPUT, "nelem=%d too large for int32 support entries", mesh->nelem);
+    if (!mesh->connectivity || !mesh->bcflag || !mesh->bfacet_offsets)
+        return fail_msg(g_create_error, DES_EINPUT, "NULL connectivity/bcflag/bfacet_offsets");
+    if (precision != DES_PREC_FP64 && precision != DES_PREC_MIXED)
+        return fail_msg(g_create_error, DES_EINPUT, "unknown precision %d", precision);
+
+    c = new des_ctx();
+    c->precision = precision;
+    c->nd = mesh->ndims;
+    c->npe = c->nd + 1;
+    c->nstr = c->nd == 3 ? 6 : 3;
+    c->nn = mesh->nnode;
+    c->ne = mesh->nelem;
+    const int nd = c->nd, npe = c->npe, nn = c->nn, ne = c->ne;
+    int rc;
+    if ((rc = set_params(c, param)) || (rc = set_material(c, mat))) {
+        g_create_error = c->err;
+        delete c;
+        return rc;
+    }
+
+    // ---- topology products on the host ----
+    const int *cn = mesh->connectivity;
+    for (long long i = 0; i < (long long)ne * npe; ++i) {
+        if (cn[i] < 0 || cn[i] >= nn) {
+            int code = fail_msg(g_create_error, DES_EINPUT, "connectivity[%lld] = %d out of range [0,%d)", i,
+                                cn[i], nn);
+            delete c;
+            return code;
+        }
+    }
+    // support lists in ascending element order (create_support, mesh.cxx:1707-1721)
+    std::vector<int> sup_off(nn + 1, 0), sup_ent((size_t)ne * npe);
+    for (long long i = 0; i < (long long)ne * npe; ++i) sup_off[cn[i] + 1]++;
+    for (int n = 0; n < nn; ++n) sup_off[n + 1] += sup_off[n];
+    {
+        std::vector<int> fill(sup_off.begin(), sup_off.end() - 1);
+        for (int e = 0; e < ne; ++e)
+            for (int i = 0; i < npe; ++i) sup_ent[fill[cn[(size_t)e * npe + i]]++] = e * 4 + i;
+    }
+    // boundary facets and the node -> facet lists (ascending global facet id)
+    const int nbf = mesh->bfacet_offsets[DES_NBDRYTYPES] - mesh->bfacet_offsets[0];
+    c->nbf = nbf;
+    std::vector<int> fac_elem(std::max(nbf, 1)), fac_f(std::max(nbf, 1)), fac_bdry(std::max(nbf, 1));
+    std::vector<int> nf_off(nn + 1, 0), nf_ent;
+    {
+        static const int F3[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
+        static const int F2[3][2] = {{1, 2}, {2, 0}, {0, 1}};
+        int q = 0;
+        for (int b = 0; b < DES_NBDRYTYPES; ++b) {
+            for (int k = mesh->bfacet_offsets[b]; k < mesh->bfacet_offsets[b + 1]; ++k, ++q) {
+                int e = mesh->bfacets[2 * k], f = mesh->bfacets[2 * k + 1];
+                if (e < 0 || e >= ne || f < 0 || f > nd) {
+                    int code = fail_msg(g_create_error, DES_EINPUT, "bad boundary facet (%d,%d)", e, f);
+                    delete c;
+                    return code;
+                }
+                fac_elem[q] = e;
+                fac_f[q] = f;
+                fac_bdry[q] = b;
+                for (int j = 0; j < nd; ++j) nf_off[cn[(size_t)e * npe + (nd == 3 ? F3[f][j] : F2[f][j])] + 1]++;
+            }
+        }
+        for (int n = 0; n < nn; ++n) nf_off[n + 1] += nf_off[n];
+        nf_ent.resize(std::max(nf_off[nn], 1));
+        std::vector<int> fill(nf_off.begin(), nf_off.end() - 1);
+        for (int qq = 0; qq < nbf; ++qq) {
+            int e = fac_elem[qq], f = fac_f[qq];
+            for (int j = 0; j < nd; ++j) nf_ent[fill[cn[(size_t)e * npe + (nd == 3 ? F3[f][j] : F2[f][j])]]++] = qq;
+        }
+    }
+
+    // ---- device ----
+    if (cudaGetDevice(&c->device) != cudaSuccess) {
+        int code = fail_msg(g_create_error, DES_ECUDA, "no CUDA device");
+        delete c;
+        return code;
+    }
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            int code = fail_msg(g_create_error, DES_ECUDA, "cudaStreamCreate failed");
+            delete c;
+            return code;
+        }
+        c->own_stream = true;
+    }
+
+    // sizes (in bytes) of every array carved from the pool
+    const size_t D = sizeof(double), I = sizeof(int);
+    struct Slot { void **dst; size_t bytes; };
+    KP &p = c->kp;
+    std::vector<Slot> slots;
+    auto add = [&](void **dst, size_t bytes) { slots.push_back({dst, align256(std::max<size_t>(bytes, 8))}); };
+    int *d_conn, *d_sup_off, *d_sup_ent, *d_nf_off, *d_nf_ent, *d_fe, *d_ff, *d_fb, *d_emark = nullptr;
+    unsigned *d_bc;
+    add((void **)&d_conn, (size_t)ne * npe * I);
+    add((void **)&d_bc, (size_t)nn * sizeof(unsigned));
+    add((void **)&d_sup_off, (size_t)(nn + 1) * I);
+    add((void **)&d_sup_ent, (size_t)ne * npe * I);
+    add((void **)&d_nf_off, (size_t)(nn + 1) * I);
+    add((void **)&d_nf_ent, nf_ent.size() * I);
+    add((void **)&d_fe, fac_elem.size() * I);
+    add((void **)&d_ff, fac_f.size() * I);
+    add((void **)&d_fb, fac_bdry.size() * I);
+    if (mat->elemmarkers && mat->nmat > 1) add((void **)&d_emark, (size_t)ne * mat->nmat * I);
+    add((void **)&p.x, (size_t)nn * nd * D);
+    add((void **)&p.x0, (size_t)nn * nd * D);
+    add((void **)&p.v, (size_t)nn * nd * D);
+    add((void **)&p.f, (size_t)nn * nd * D);
+    add((void **)&p.T, (size_t)nn * D);
+    add((void **)&p.mass, (size_t)nn * D);
+    add((void **)&p.tmass, (size_t)nn * D);
+    add((void **)&p.vol_n, (size_t)nn * D);
+    add((void **)&p.ntmp, (size_t)nn * D);
+    add((void **)&c->d_tdot, (size_t)nn * D);
+    add((void **)&p.stress, (size_t)ne * c->nstr * D);
+    add((void **)&p.strain, (size_t)ne * c->nstr * D);
+    add((void **)&p.srate, (size_t)ne * c->nstr * D);
+    add((void **)&p.pls, (size_t)ne * D);
+    add((void **)&p.dpls, (size_t)ne * D);
+    add((void **)&p.syy, (size_t)ne * D);
+    add((void **)&p.dp, (size_t)ne * D);
+    add((void **)&p.edvoldt, (size_t)ne * D);
+    add((void **)&p.vol, (size_t)ne * D);
+    add((void **)&p.vol_old, (size_t)ne * D);
+    add((void **)&p.shp, (size_t)ne * npe * nd * D);
+    add((void **)&c->d_rho, (size_t)ne * D);
+    add((void **)&p.fv, (size_t)std::max(nbf, 1) * nd * D);
+    add((void **)&p.clk, sizeof(Clock));
+    add((void **)&p.err, sizeof(unsigned));
+    add((void **)&c->d_red, 2 * sizeof(unsigned long long));
+    c->stage_doubles = std::max((size_t)ne * std::max(c->nstr, npe), (size_t)nn * nd);
+    add((void **)&c->d_stage, c->stage_doubles * D);
+    size_t total = 0;
+    for (auto &s : slots) total += s.bytes;
+    cudaError_t ce = cudaMalloc((void **)&c->pool, total);
+    if (ce != cudaSuccess) {
+        int code = fail_msg(g_create_error, DES_ENOMEM, "cudaMalloc(%zu bytes): %s", total, cudaGetErrorString(ce));
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return code;
+    }
+    c->pool_bytes = total;
+    ce = cudaMemset(c->pool, 0, total);
+    if (ce != cudaSuccess) {
+        int code = fail_msg(g_create_error, DES_ECUDA, "cudaMemset: %s", cudaGetErrorString(ce));
+        cudaFree(c->pool);
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return code;
+    }
+    {
+        size_t off = 0;
+        for (auto &s : slots) {
+            *s.dst = c->pool + off;
+            off += s.bytes;
+        }
+    }
+    p.nd = nd;
+    p.npe = npe;
+    p.nstr = c->nstr;
+    p.nn = nn;
+    p.ne = ne;
+    p.nbf = nbf;
+    p.conn = d_conn;
+    p.bcflag = d_bc;
+    p.sup_off = d_sup_off;
+    p.sup_ent = d_sup_ent;
+    p.nf_off = d_nf_off;
+    p.nf_ent = d_nf_ent;
+    p.fac_elem = d_fe;
+    p.fac_f = d_ff;
+    p.fac_bdry = d_fb;
+    p.emark = d_emark;
+    p.rho_e = nullptr;
+    p.tdot = p.ntmp;
+    for (int i = 0; i < DES_NBDRYTYPES; ++i)
+        for (int d = 0; d < 3; ++d) {
+            p.bnormals[i][d] = mesh->bnormals[i][d];
+            for (int j = 0; j < DES_NBDRYTYPES; ++j) p.edge_vectors[i][j][d] = mesh->edge_vectors[i][j][d];
+        }
+
+    // uploads (synchronous: creation time only)
+    std::vector<int> conn_soa((size_t)ne * npe);
+    for (int e = 0; e < ne; ++e)
+        for (int i = 0; i < npe; ++i) conn_soa[(size_t)i * ne + e] = cn[(size_t)e * npe + i];
+    cudaError_t e1 = cudaSuccess;
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        if (e1 == cudaSuccess && bytes) e1 = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    up(d_conn, conn_soa.data(), conn_soa.size() * I);
+    up(d_bc, mesh->bcflag, (size_t)nn * sizeof(unsigned));
+    up(d_sup_off, sup_off.data(), sup_off.size() * I);
+    up(d_sup_ent, sup_ent.data(), sup_ent.size() * I);
+    up(d_nf_off, nf_off.data(), nf_off.size() * I);
+    up(d_nf_ent, nf_ent.data(), nf_ent.size() * I);
+    up(d_fe, fac_elem.data(), fac_elem.size() * I);
+    up(d_ff, fac_f.data(), fac_f.size() * I);
+    up(d_fb, fac_bdry.data(), fac_bdry.size() * I);
+    if (d_emark) {
+        std::vector<int> em((size_t)ne * mat->nmat);
+        for (int e = 0; e < ne; ++e)
+            for (int m = 0; m < mat->nmat; ++m) em[(size_t)m * ne + e] = mat->elemmarkers[(size_t)e * mat->nmat + m];
+        up(d_emark, em.data(), em.size() * I);
+    }
+    if (e1 == cudaSuccess) {
+        Clock ck{};
+        ck.red_minh = ck.red_maxwell = ck.red_diffusion = ~0ull;
+        e1 = cudaMemcpy(p.clk, &ck, sizeof ck, cudaMemcpyHostToDevice);
+    }
+    if (e1 != cudaSuccess) {
+        int code = fail_msg(g_create_error, DES_ECUDA, "device setup: %s", cudaGetErrorString(e1));
+        cudaFree(c->pool);
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return code;
+    }
+    *out = c;
+    return DES_OK;
+}
+
+int des_destroy(des_ctx *c)
+{
+    if (!c) return DES_OK;
+    cudaStreamSynchronize(c->stream);
+    invalidate_graph(c);
+    for (int k = 0; k < DES_EF_COUNT; ++k)
+        if (c->d_ef[k]) cudaFree(c->d_ef[k]);
+    cudaFree(c->pool);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return DES_OK;
+}
+
+int des_device_status(des_ctx *c, unsigned *bits)
+{
+    if (!c || !bits) return DES_EINPUT;
+    unsigned h = 0;
+    CK(cudaMemcpyAsync(&h, c->kp.err, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemsetAsync(c->kp.err, 0, sizeof(unsigned), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *bits = h & 0xffu;
+    if (h & 0x100u) {
+        fail_msg(c->err, DES_ERUNTIME, "Error: dt <= 0!");
+        return DES_ERUNTIME;
+    }
+    return DES_OK;
+}
+
+int des_set_params(des_ctx *c, const des_params *prm)
+{
+    if (!c || !prm) return DES_EINPUT;
+    return set_params(c, prm);
+}
+
+int des_set_elem_field(des_ctx *c, int field, const double *values)
+{
+    if (!c || field < 0 || field >= DES_EF_COUNT) return DES_EINPUT;
+    invalidate_graph(c);
+    if (!values) {
+        if (c->d_ef[field]) {
+            CK(cudaStreamSynchronize(c->stream));
+            cudaFree(c->d_ef[field]);
+        }
+        c->d_ef[field] = nullptr;
+        c->kp.ef[field] = nullptr;
+        return DES_OK;
+    }
+    if (!c->d_ef[field]) CK(cudaMalloc((void **)&c->d_ef[field], (size_t)c->ne * sizeof(double)));
+    CK(cudaMemcpyAsync(c->d_ef[field], values, (size_t)c->ne * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->kp.ef[field] = c->d_ef[field];
+    return DES_OK;
+}
+
+// ---- state transfer ----
+namespace {
+
+int put_field(des_ctx *c, const double *host, double *dev, int n, int ncomp)
+{
+    size_t bytes = (size_t)n * ncomp * sizeof(double);
+    if (ncomp == 1) {
+        CK(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, c->stream));
+        return DES_OK;
+    }
+    CK(cudaMemcpyAsync(c->d_stage, host, bytes, cudaMemcpyHostToDevice, c->stream));
+    return check_launch(c, launch_aos_to_soa(c->d_stage, dev, n, ncomp, c->stream));
+}
+
+int get_field(des_ctx *c, double *host, const double *dev, int n, int ncomp)
+{
+    size_t bytes = (size_t)n * ncomp * sizeof(double);
+    if (ncomp == 1) {
+        CK(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->stream));
+        return DES_OK;
+    }
+    int rc = check_launch(c, launch_soa_to_aos(dev, c->d_stage, n, ncomp, c->stream));
+    if (rc) return rc;
+    // stream order keeps the staging buffer's next writer behind this copy
+    CK(cudaMemcpyAsync(host, c->d_stage, bytes, cudaMemcpyDeviceToHost, c->stream));
+    return DES_OK;
+}
+
+}  // namespace
+
+int des_upload_state(des_ctx *c, const des_host_state *st)
+{
+    if (!c || !st) return DES_EINPUT;
+    if (!st->coord || !st->vel || !st->temperature || !st->volume_old || !st->stress || !st->strain ||
+        !st->plstrain)
+        return fail_msg(c->err, DES_EINPUT, "upload: coord, vel, temperature, volume_old, stress, strain and "
+                        "plstrain are required");
+    KP &p = c->kp;
+    const int nn = c->nn, ne = c->ne, nd = c->nd, npe = c->npe, nstr = c->nstr;
+    int rc;
+#define PUT(h, d, n, k)                                               \
+    do {                                                              \
+        if ((rc = put_field(c, (h), (d), (n), (k))) != DES_OK) return rc; \
+    } while (0)
+#define ZERO(d, bytes) CK(cudaMemsetAsync((d), 0, (bytes), c->stream))
+    PUT(st->coord, p.x, nn, nd);
+    if (st->coord0) PUT(st->coord0, p.x0, nn, nd);
+    else CK(cudaMemcpyAsync(p.x0, p.x, (size_t)nn * nd * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    PUT(st->vel, p.v, nn, nd);
+    if (st->force) PUT(st->force, p.f, nn, nd);
+    else ZERO(p.f, (size_t)nn * nd * sizeof(double));
+    PUT(st->temperature, p.T, nn, 1);
+    PUT(st->volume_old, p.vol_old, ne, 1);
+    PUT(st->stress, p.stress, ne, nstr);
+    PUT(st->strain, p.strain, ne, nstr);
+    PUT(st->plstrain, p.pls, ne, 1);
+    if (st->strain_rate) PUT(st->strain_rate, p.srate, ne, nstr);
+    else ZERO(p.srate, (size_t)ne * nstr * sizeof(double));
+    if (st->delta_plstrain) PUT(st->delta_plstrain, p.dpls, ne, 1);
+    else ZERO(p.dpls, (size_t)ne * sizeof(double));
+    if (st->stressyy) PUT(st->stressyy, p.syy, ne, 1);
+    else ZERO(p.syy, (size_t)ne * sizeof(double));
+    if (st->dpressure) PUT(st->dpressure, p.dp, ne, 1);
+    else ZERO(p.dp, (size_t)ne * sizeof(double));
+    if (st->edvoldt) PUT(st->edvoldt, p.edvoldt, ne, 1);
+    else ZERO(p.edvoldt, (size_t)ne * sizeof(double));
+    if (st->ntmp) PUT(st->ntmp, p.ntmp, nn, 1);
+    else ZERO(p.ntmp, (size_t)nn * sizeof(double));
+    {
+        Clock ck{};
+        ck.time = st->time;
+        ck.dt = st->dt;
+        ck.steps = st->steps;
+        ck.red_minh = ck.red_maxwell = ck.red_diffusion = ~0ull;
+        CK(cudaMemcpyAsync(p.clk, &ck, sizeof ck, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));   // ck lives on this stack frame
+    }
+    KP q = p;   // per-function form
+    if (st->volume) PUT(st->volume, p.vol, ne, 1);
+    else if ((rc = check_launch(c, launch_geometry(q, c->stream, GEO_VOLUME)))) return rc;
+    if (st->shpdx && st->shpdz && (nd == 2 || st->shpdy)) {
+        PUT(st->shpdx, p.shp, ne, npe);
+        if (nd == 3) PUT(st->shpdy, p.shp + (size_t)ne * npe, ne, npe);
+        PUT(st->shpdz, p.shp + (size_t)(nd - 1) * ne * npe, ne, npe);
+    } else if ((rc = check_launch(c, launch_geometry(q, c->stream, GEO_SHAPE)))) return rc;
+    if (st->mass && st->tmass && st->volume_n) {
+        PUT(st->mass, p.mass, nn, 1);
+        PUT(st->tmass, p.tmass, nn, 1);
+        PUT(st->volume_n, p.vol_n, nn, 1);
+    } else if ((rc = check_launch(c, launch_mass(q, c->stream)))) return rc;
+#undef PUT
+#undef ZERO
+    CK(cudaStreamSynchronize(c->stream));
+    c->has_state = true;
+    return DES_OK;
+}
+
+int des_download_state(des_ctx *c, des_host_state *st)
+{
+    if (!c || !st) return DES_EINPUT;
+    KP &p = c->kp;
+    const int nn = c->nn, ne = c->ne, nd = c->nd, npe = c->npe, nstr = c->nstr;
+    int rc;
+#define GET(h, d, n, k) \
+    if ((h) && (rc = get_field(c, (h), (d), (n), (k))) != DES_OK) return rc
+    GET(st->coord, p.x, nn, nd);
+    GET(st->coord0, p.x0, nn, nd);
+    GET(st->vel, p.v, nn, nd);
+    GET(st->force, p.f, nn, nd);
+    GET(st->temperature, p.T, nn, 1);
+    GET(st->mass, p.mass, nn, 1);
+    GET(st->tmass, p.tmass, nn, 1);
+    GET(st->volume_n, p.vol_n, nn, 1);
+    GET(st->ntmp, p.ntmp, nn, 1);
+    GET(st->volume, p.vol, ne, 1);
+    GET(st->volume_old, p.vol_old, ne, 1);
+    GET(st->stress, p.stress, ne, nstr);
+    GET(st->strain, p.strain, ne, nstr);
+    GET(st->strain_rate, p.srate, ne, nstr);
+    GET(st->plstrain, p.pls, ne, 1);
+    GET(st->delta_plstrain, p.dpls, ne, 1);
+    GET(st->stressyy, p.syy, ne, 1);
+    GET(st->dpressure, p.dp, ne, 1);
+    GET(st->edvoldt, p.edvoldt, ne, 1);
+    GET(st->shpdx, p.shp, ne, npe);
+    if (nd == 3) GET(st->shpdy, p.shp + (size_t)ne * npe, ne, npe);
+    GET(st->shpdz, p.shp + (size_t)(nd - 1) * ne * npe, ne, npe);
+#undef GET
+    Clock ck;
+    CK(cudaMemcpyAsync(&ck, p.clk, sizeof ck, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    st->time = ck.time;
+    st->dt = ck.dt;
+    st->steps = ck.steps;
+    return DES_OK;
+}
+
+int des_get_clock(des_ctx *c, double *time, double *dt, int *steps)
+{
+    if (!c) return DES_EINPUT;
+    Clock ck;
+    CK(cudaMemcpyAsync(&ck, c->kp.clk, sizeof ck, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (time) *time = ck.time;
+    if (dt) *dt = ck.dt;
+    if (steps) *steps = ck.steps;
+    return DES_OK;
+}
+
+int des_set_clock(des_ctx *c, double time, double dt, int steps)
+{
+    if (!c) return DES_EINPUT;
+    Clock ck;
+    CK(cudaMemcpyAsync(&ck, c->kp.clk, sizeof ck, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    ck.time = time;
+    ck.dt = dt;
+    ck.steps = steps;
+    CK(cudaMemcpyAsync(c->kp.clk, &ck, sizeof ck, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DES_OK;
+}
+
+// ---- per-function entry points ----
+#define PERFN(name, body)                     \
+    int name(des_ctx *c)                      \
+    {                                         \
+        if (!c) return DES_EINPUT;            \
+        const KP &p = c->kp;                  \
+        cudaStream_t s = c->stream;           \
+        int n = 0;                            \
+        body;                                 \
+        return check_launch(c, n);            \
+    }
+
+PERFN(des_update_temperature, n += launch_heat_gather(p, s); n += launch_temperature_update(p, s))
+PERFN(des_update_strain_rate, n += launch_strain_rate(p, s, false))
+PERFN(des_compute_dvoldt, n += launch_dvoldt(p, s))
+PERFN(des_compute_edvoldt, n += launch_edvoldt(p, s))
+PERFN(des_update_stress, n += launch_update_stress(p, s, false))
+PERFN(des_NMD_stress, n += launch_nmd_gather(p, s); n += launch_nmd_correct(p, s, false))
+PERFN(des_update_force, n += launch_facet_forces(p, s); n += launch_force(p, s, false))
+PERFN(des_update_velocity, n += launch_velocity(p, s))
+PERFN(des_apply_vbcs, n += launch_vbcs(p, s))
+PERFN(des_update_coordinate, n += launch_coordinate(p, s))
+PERFN(des_swap_volume, n += launch_geometry(p, s, GEO_COPY_OLD))
+PERFN(des_compute_volume, n += launch_geometry(p, s, GEO_VOLUME))
+PERFN(des_compute_mass, n += launch_mass(p, s))
+PERFN(des_compute_shape_fn, n += launch_geometry(p, s, GEO_SHAPE))
+PERFN(des_rotate_stress, n += launch_geometry(p, s, GEO_ROTATE))
+PERFN(des_update_mesh, n += launch_coordinate(p, s);
+      n += launch_geometry(p, s, GEO_COPY_OLD | GEO_VOLUME); n += launch_mass(p, s);
+      n += launch_geometry(p, s, GEO_SHAPE))
+
+int des_compute_dt(des_ctx *c, double *dt_out)
+{
+    if (!c) return DES_EINPUT;
+    int rc = check_launch(c, launch_geometry(c->kp, c->stream, GEO_DT) + launch_dt_finalize(c->kp, c->stream, false));
+    if (rc) return rc;
+    double dt;
+    rc = des_get_clock(c, nullptr, &dt, nullptr);
+    if (rc) return rc;
+    if (dt_out) *dt_out = dt;
+    unsigned bits;
+    return des_device_status(c, &bits);
+}
+
+int des_worst_elem_quality(des_ctx *c, double *quality, int *elem)
+{
+    if (!c) return DES_EINPUT;
+    unsigned long long init[2] = {~0ull, ~0ull}, res[2];
+    CK(cudaMemcpyAsync(c->d_red, init, sizeof init, cudaMemcpyHostToDevice, c->stream));
+    int rc = check_launch(c, launch_quality(c->kp, c->stream, c->d_red));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(res, c->d_red, sizeof res, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double q;
+    memcpy(&q, &res[0], sizeof q);
+    int w = (int)res[1];
+    if (!(q < 1)) {   // worst_elem_quality starts from q = 1, worst = 0
+        q = 1;
+        w = 0;
+    }
+    if (quality) *quality = q;
+    if (elem) *elem = w;
+    return DES_OK;
+}
+
+// ---- the fused step ----
+namespace {
+
+int enqueue_step(des_ctx *c)
+{
+    const KP p = step_kp(c);
+    cudaStream_t s = c->stream;
+    int n = 0;
+    const bool thermal = p.prm.has_thermal_diffusion != 0;
+    n += launch_strain_rate(p, s, true);
+    if (thermal) {
+        n += launch_heat_and_dvoldt(p, s);
+        n += launch_temperature_update(p, s);
+    } else {
+        n += launch_dvoldt(p, s);
+    }
+    n += launch_update_stress(p, s, true);
+    n += launch_nmd_gather(p, s);
+    n += launch_nmd_correct(p, s, true);
+    n += launch_force(p, s, true);
+    int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP;
+    if (p.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;
+    n += launch_geometry(p, s, geo);
+    n += launch_mass(p, s);
+    n += launch_dt_finalize(p, s, true);
+    return n;
+}
+
+int build_step_graph(des_ctx *c)
+{
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int n = enqueue_step(c);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&c->step_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->step_exec = nullptr;
+        return cuda_fail(c, e, "cudaGraphInstantiate");
+    }
+    c->step_kernels = n;
+    return DES_OK;
+}
+
+}  // namespace
+
+int des_step(des_ctx *c, int nsteps)
+{
+    if (!c || nsteps < 0) return DES_EINPUT;
+    if (!c->has_state) return fail_msg(c->err, DES_EINPUT, "des_step before des_upload_state");
+    if (!c->step_exec) {
+        int rc = build_step_graph(c);
+        if (rc) return rc;
+    }
+    for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(c->step_exec, c->stream));
+    c->launches += (long long)nsteps * c->step_kernels;
+    return DES_OK;
+}
+
+int des_step_host(des_ctx *c, des_host_state *st, int nsteps)
+{
+    int rc = des_upload_state(c, st);
+    if (rc) return rc;
+    if ((rc = des_step(c, nsteps))) return rc;
+    return des_download_state(c, st);
+}
+
+int des_synchronize(des_ctx *c)
+{
+    if (!c) return DES_EINPUT;
+    CK(cudaStreamSynchronize(c->stream));
+    return DES_OK;
+}
+
+int des_launch_count(des_ctx *c, long long *count)
+{
+    if (!c || !count) return DES_EINPUT;
+    *count = c->launches;
+    return DES_OK;
+}
+
+}  // extern "C"

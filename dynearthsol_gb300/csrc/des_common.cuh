@@ -1,0 +1,328 @@
+// des_common.cuh -- device data layout and shared device helpers of the
+// GB300 explicit-step library.
+//
+// Layout in HBM (structure of arrays, component-major):
+//   node fields   x[d*nn + n], v[d*nn + n], f[d*nn + n], T[n], mass[n], ...
+//   element fields stress[c*ne + e] (c = XX,YY,ZZ,XY,XZ,YZ; 2D: XX,ZZ,XZ),
+//                  shp[(k*npe + i)*ne + e] (k = x,y,z derivative, i = local node)
+//   connectivity   conn[i*ne + e]
+//   support CSR    sup_off[nn+1], sup_ent[] = e*4 + local slot, ascending e
+//                  (the reference's support lists, mesh.cxx:1707-1721, in the
+//                  serial summation order of its element loops)
+// Every node quantity the reference scatters element by element is gathered
+// here per node in that same order: no atomics, reproducible results.
+#pragma once
+
+#include <cstdint>
+#include <cfloat>
+#include <cmath>
+
+#include "../../include/desgpu.h"
+
+#define DES_MAXMAT 8
+
+namespace des {
+
+constexpr unsigned BOUNDX0 = 1u << 0, BOUNDX1 = 1u << 1, BOUNDY0 = 1u << 2, BOUNDY1 = 1u << 3,
+                   BOUNDZ0 = 1u << 4, BOUNDZ1 = 1u << 5, BOUND_ANY = 1023u;
+
+// constants.hpp:73-74
+constexpr double DEG2RAD = 3.1415926535897932384626433832795 / 180;
+
+// device clock of a context (Variables::time, dt, steps)
+struct Clock {
+    double time;
+    double dt;
+    int steps;
+    int pad;
+    // compute_dt accumulators: min over elements as ordered bit patterns
+    unsigned long long red_minh;
+    unsigned long long red_maxwell;
+    unsigned long long red_diffusion;
+    double last_dt_terms[4];   // maxwell, diffusion, advection, elastic
+};
+
+// material table (MatProps, matprops.hpp:19-76) with nmat <= DES_MAXMAT
+struct MatC {
+    int rheol_type, nmat, is_plane_strain;
+    unsigned scalar_mask;
+    double visc_min, visc_max, tension_max, therm_diff_max;
+    double rho0[DES_MAXMAT], alpha[DES_MAXMAT];
+    double bulk_modulus[DES_MAXMAT], shear_modulus[DES_MAXMAT];
+    double visc_exponent[DES_MAXMAT], visc_coefficient[DES_MAXMAT], visc_activation_energy[DES_MAXMAT];
+    double heat_capacity[DES_MAXMAT], therm_cond[DES_MAXMAT], radiogenic_heating[DES_MAXMAT];
+    double pls0[DES_MAXMAT], pls1[DES_MAXMAT];
+    double cohesion0[DES_MAXMAT], cohesion1[DES_MAXMAT];
+    double friction_angle0[DES_MAXMAT], friction_angle1[DES_MAXMAT];
+    double dilation_angle0[DES_MAXMAT], dilation_angle1[DES_MAXMAT];
+};
+
+// Everything a kernel needs, passed by value.
+struct KP {
+    int nd, npe, nstr, nn, ne, nbf;
+    // mesh
+    const int *conn;
+    const unsigned *bcflag;
+    const int *sup_off, *sup_ent;
+    const int *nf_off, *nf_ent;          // node -> boundary facets (ascending facet id)
+    const int *fac_elem, *fac_f, *fac_bdry;
+    const int *emark;                    // [nmat][ne] marker counts, or null
+    // node fields
+    double *x, *x0, *v, *f, *T, *mass, *tmass, *vol_n, *ntmp;
+    // element fields
+    double *stress, *strain, *srate, *pls, *dpls, *syy, *dp, *edvoldt, *vol, *vol_old, *shp;
+    double *rho_e;                       // per-element density of the step (scratch), or null
+    double *tdot;                        // node scratch for the heat gather (ntmp outside the fused step)
+    double *fv;                          // [nd][nbf] per-facet stress-BC force (scratch)
+    const double *ef[DES_EF_COUNT];      // per-element overrides or null
+    Clock *clk;
+    unsigned *err;
+    // parameters
+    des_params prm;
+    MatC mat;
+    double bnormals[DES_NBDRYTYPES][3];
+    double edge_vectors[DES_NBDRYTYPES][DES_NBDRYTYPES][3];
+};
+
+__device__ __forceinline__ double dmax_(double a, double b) { return (a < b) ? b : a; }  // std::max
+__device__ __forceinline__ double dmin_(double a, double b) { return (b < a) ? b : a; }  // std::min
+
+template <int ND>
+__device__ __forceinline__ double trace_(const double *s)
+{
+    if (ND == 3) return s[0] + s[1] + s[2];
+    return s[0] + s[1];
+}
+
+// utils.hpp:110-128
+template <int ND>
+__device__ __forceinline__ double second_invariant2_(const double *t)
+{
+    if (ND == 3) {
+        double a = (t[0] + t[1] + t[2]) / 3;
+        return (0.5 * ((t[0] - a) * (t[0] - a) + (t[1] - a) * (t[1] - a) + (t[2] - a) * (t[2] - a))
+                + t[3] * t[3] + t[4] * t[4] + t[5] * t[5]);
+    }
+    return 0.25 * (t[0] - t[1]) * (t[0] - t[1]) + t[2] * t[2];
+}
+
+template <int ND>
+__device__ __forceinline__ double second_invariant_(const double *t)
+{
+    return sqrt(second_invariant2_<ND>(t));
+}
+
+// ------------------------------------------------------------------
+// material properties (matprops.cxx:103-414)
+// ------------------------------------------------------------------
+__device__ __forceinline__ int mcount(const KP &p, int e, int m)
+{
+    if (p.emark) return p.emark[(size_t)m * p.ne + e];
+    return m == 0 ? 1 : 0;
+}
+
+__device__ __forceinline__ double hmean(const KP &p, const double *s, int bit, int e)
+{
+    if (p.mat.nmat == 1 || ((p.mat.scalar_mask >> bit) & 1u)) return s[0];
+    double result = 0;
+    int m = 0;
+    for (int i = 0; i < p.mat.nmat; i++) {
+        int n = mcount(p, e, i);
+        result += n / s[i];
+        m += n;
+    }
+    return m / result;
+}
+
+__device__ __forceinline__ double amean(const KP &p, const double *s, int bit, int e)
+{
+    if (p.mat.nmat == 1 || ((p.mat.scalar_mask >> bit) & 1u)) return s[0];
+    double result = 0;
+    int m = 0;
+    for (int i = 0; i < p.mat.nmat; i++) {
+        int n = mcount(p, e, i);
+        result += n * s[i];
+        m += n;
+    }
+    return result / m;
+}
+
+__device__ __forceinline__ double m_bulkm(const KP &p, int e) { return hmean(p, p.mat.bulk_modulus, 0, e); }
+__device__ __forceinline__ double m_shearm(const KP &p, int e)
+{
+    if (p.ef[DES_EF_SHEAR_MODULUS]) return p.ef[DES_EF_SHEAR_MODULUS][e];
+    return hmean(p, p.mat.shear_modulus, 1, e);
+}
+__device__ __forceinline__ double m_cp(const KP &p, int e) { return amean(p, p.mat.heat_capacity, 2, e); }
+__device__ __forceinline__ double m_hr(const KP &p, int e) { return amean(p, p.mat.radiogenic_heating, 3, e); }
+__device__ __forceinline__ double m_k(const KP &p, int e)
+{
+    if (p.ef[DES_EF_THERM_COND]) return p.ef[DES_EF_THERM_COND][e];
+    return amean(p, p.mat.therm_cond, 4, e);
+}
+
+template <int NPE>
+__device__ __forceinline__ double elem_avg_T(const KP &p, int e)
+{
+    double t = 0;
+#pragma unroll
+    for (int i = 0; i < NPE; ++i) t += p.T[p.conn[(size_t)i * p.ne + e]];
+    return t / NPE;
+}
+
+// MatProps::rho (matprops.cxx:376-397) given the element's mean temperature
+__device__ __forceinline__ double m_rho_T(const KP &p, int e, double T)
+{
+    const double celsius0 = 273;
+    double TinCelsius = T - celsius0;
+    double result = 0;
+    int n = 0;
+    for (int m = 0; m < p.mat.nmat; m++) {
+        int k = mcount(p, e, m);
+        result += p.mat.rho0[m] * (1 - p.mat.alpha[m] * TinCelsius) * k;
+        n += k;
+    }
+    return result / n;
+}
+
+template <int ND>
+__device__ __forceinline__ double m_rho(const KP &p, int e)
+{
+    return m_rho_T(p, e, elem_avg_T<ND + 1>(p, e));
+}
+
+// MatProps::visc (matprops.cxx:276-312); edot = the element's strain rate
+template <int ND>
+__device__ double m_visc(const KP &p, int e, const double *edot)
+{
+    double v;
+    if (p.ef[DES_EF_LOG10_VISC]) {
+        v = pow(10.0, p.ef[DES_EF_LOG10_VISC][e]);
+    } else {
+        const double gas_constant = 8.3144;
+        const double min_strain_rate = 1e-30;
+        double T = elem_avg_T<ND + 1>(p, e);
+        double ed = second_invariant_<ND>(edot);
+        ed = dmax_(ed, min_strain_rate);
+        double result = 0;
+        int n = 0;
+        for (int m = 0; m < p.mat.nmat; m++) {
+            double pw = 1 / p.mat.visc_exponent[m] - 1;
+            double pw1 = -1 / p.mat.visc_exponent[m];
+            double visc0 = 0.25 * pow(ed, pw) * pow(0.75 * p.mat.visc_coefficient[m], pw1)
+                * exp(p.mat.visc_activation_energy[m] / (p.mat.visc_exponent[m] * gas_constant * T)) * 1e6;
+            int k = mcount(p, e, m);
+            result += k / visc0;
+            n += k;
+        }
+        v = n / result;
+    }
+    return dmin_(dmax_(v, p.mat.visc_min), p.mat.visc_max);
+}
+
+// MatProps::plastic_weakening + plastic_props (matprops.cxx:315-373)
+__device__ inline void m_plastic_props(const KP &p, int e, double pls, double &amc, double &anphi,
+                                double &anpsi, double &hardn, double &ten_max)
+{
+    double cc = 0, f = 0, d = 0, h = 0;
+    int n = 0;
+    for (int m = 0; m < p.mat.nmat; m++) {
+        int k = mcount(p, e, m);
+        if (k == 0) continue;
+        n += k;
+        double c0 = p.ef[DES_EF_COHESION0] ? p.ef[DES_EF_COHESION0][e] : p.mat.cohesion0[m];
+        double c1 = p.ef[DES_EF_COHESION1] ? p.ef[DES_EF_COHESION1][e] : p.mat.cohesion1[m];
+        double f0 = p.ef[DES_EF_FRICTION0] ? p.ef[DES_EF_FRICTION0][e] : p.mat.friction_angle0[m];
+        double f1 = p.ef[DES_EF_FRICTION1] ? p.ef[DES_EF_FRICTION1][e] : p.mat.friction_angle1[m];
+        double d0 = p.mat.dilation_angle0[m], d1 = p.mat.dilation_angle1[m];
+        double l0 = p.mat.pls0[m], l1 = p.mat.pls1[m];
+        if (pls < l0) {
+            cc += c0 * k;
+            f += f0 * k;
+            d += d0 * k;
+            h += 0;
+        } else if (pls < l1) {
+            double q = (pls - l0) / (l1 - l0);
+            cc += (c0 + q * (c1 - c0)) * k;
+            f += (f0 + q * (f1 - f0)) * k;
+            d += (d0 + q * (d1 - d0)) * k;
+            h += (c1 - c0) / (l1 - l0) * k;
+        } else {
+            cc += c1 * k;
+            f += f1 * k;
+            d += d1 * k;
+            h += 0;
+        }
+    }
+    double cohesion = cc / n, phi = f / n, psi = d / n;
+    hardn = h / n;
+    double sphi = sin(phi * DEG2RAD);
+    double spsi = sin(psi * DEG2RAD);
+    anphi = (1 + sphi) / (1 - sphi);
+    anpsi = (1 + spsi) / (1 - spsi);
+    amc = 2 * cohesion * sqrt(anphi);
+    ten_max = (phi == 0) ? p.mat.tension_max : dmin_(p.mat.tension_max, cohesion / tan(phi * DEG2RAD));
+}
+
+// ref_pressure option 0 (matprops.cxx:190-202)
+__device__ __forceinline__ double ref_pressure_(const KP &p, double z)
+{
+    double depth = -z;
+    return p.mat.rho0[0] * p.prm.gravity * depth;
+}
+
+// ------------------------------------------------------------------
+// mesh helpers
+// ------------------------------------------------------------------
+__device__ __forceinline__ int conn_at(const KP &p, int i, int e) { return p.conn[(size_t)i * p.ne + e]; }
+
+__device__ __forceinline__ double shp_at(const KP &p, int k, int i, int e)
+{
+    return p.shp[((size_t)k * p.npe + i) * p.ne + e];
+}
+
+// tetrahedron_volume (geometry.cxx:29-49)
+__device__ __forceinline__ double tet_volume(const double *d0, const double *d1, const double *d2,
+                                             const double *d3)
+{
+    double x01 = d0[0] - d1[0], x12 = d1[0] - d2[0], x23 = d2[0] - d3[0];
+    double y01 = d0[1] - d1[1], y12 = d1[1] - d2[1], y23 = d2[1] - d3[1];
+    double z01 = d0[2] - d1[2], z12 = d1[2] - d2[2], z23 = d2[2] - d3[2];
+    return (x01 * (y23 * z12 - y12 * z23) + x12 * (y01 * z23 - y23 * z01) + x23 * (y12 * z01 - y01 * z12)) / 6;
+}
+
+// triangle_area (geometry.cxx:53-83)
+template <int ND>
+__device__ __forceinline__ double tri_area(const double *a, const double *b, const double *c)
+{
+    double ab0 = b[0] - a[0], ab1 = b[1] - a[1];
+    double ac0 = c[0] - a[0], ac1 = c[1] - a[1];
+    if (ND == 2) return fabs(ab0 * ac1 - ab1 * ac0) / 2;
+    double ab2 = b[2] - a[2], ac2 = c[2] - a[2];
+    double d0 = ab1 * ac2 - ab2 * ac1;
+    double d1 = ab2 * ac0 - ab0 * ac2;
+    double d2 = ab0 * ac1 - ab1 * ac0;
+    return sqrt(d0 * d0 + d1 * d1 + d2 * d2) / 2;
+}
+
+template <int ND>
+__device__ __forceinline__ void load_node_x(const KP &p, int n, double *c)
+{
+#pragma unroll
+    for (int d = 0; d < ND; ++d) c[d] = p.x[(size_t)d * p.nn + n];
+}
+
+template <int ND>
+__device__ __forceinline__ void load_node_v(const KP &p, int n, double *c)
+{
+#pragma unroll
+    for (int d = 0; d < ND; ++d) c[d] = p.v[(size_t)d * p.nn + n];
+}
+
+__device__ __forceinline__ void set_err(const KP &p, unsigned bits) { atomicOr(p.err, bits); }
+
+// positive doubles compare like their bit patterns
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+__device__ __forceinline__ double bitsd(unsigned long long b) { return __longlong_as_double((long long)b); }
+
+}  // namespace des

@@ -1,0 +1,1025 @@
+// des_kernels.cu -- sm_103a kernels of the explicit time step.
+//
+// Element kernels run one thread per element (SoA loads coalesce across a
+// warp); node kernels run one thread per node and gather the contributions
+// of the node's support elements in ascending element order -- the order in
+// which the reference's serial element loops scatter them -- so every nodal
+// sum is reproducible and matches the reference's serial order.
+//
+// All arithmetic is FP64 and written in the reference's expression order
+// (the library is compiled without FMA contraction), so FP64 results track
+// the reference's CPU run to the last few ulps of the transcendental
+// functions.
+#include "des_kernels.cuh"
+#include "des_rheology.cuh"
+
+namespace des {
+
+constexpr int TPB = 256;
+
+static inline int nblocks(long long n, int tpb = TPB)
+{
+    long long b = (n + tpb - 1) / tpb;
+    return (int)(b < 1 ? 1 : b);
+}
+
+// ==================================================================
+// strain rate (fields.cxx:166-232)
+// ==================================================================
+template <int ND>
+__device__ __forceinline__ void strain_rate_elem(const KP &p, int e, double *s)
+{
+    constexpr int NPE = ND + 1;
+    double v[NPE][ND];
+    double sx[NPE], sy[NPE], sz[NPE];
+#pragma unroll
+    for (int i = 0; i < NPE; ++i) {
+        int n = conn_at(p, i, e);
+        load_node_v<ND>(p, n, v[i]);
+        sx[i] = shp_at(p, 0, i, e);
+        if (ND == 3) sy[i] = shp_at(p, 1, i, e);
+        sz[i] = shp_at(p, ND - 1, i, e);
+    }
+    if (ND == 3) {
+        s[0] = 0;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) s[0] += v[i][0] * sx[i];
+        s[1] = 0;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) s[1] += v[i][1] * sy[i];
+        s[2] = 0;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) s[2] += v[i][ND - 1] * sz[i];
+        s[3] = 0;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) s[3] += 0.5 * (v[i][0] * sy[i] + v[i][1] * sx[i]);
+        s[4] = 0;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) s[4] += 0.5 * (v[i][0] * sz[i] + v[i][ND - 1] * sx[i]);
+        s[5] = 0;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) s[5] += 0.5 * (v[i][1] * sz[i] + v[i][ND - 1] * sy[i]);
+    } else {
+        s[0] = 0;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) s[0] += v[i][0] * sx[i];
+        s[1] = 0;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) s[1] += v[i][ND - 1] * sz[i];
+        s[2] = 0;
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) s[2] += 0.5 * (v[i][0] * sz[i] + v[i][ND - 1] * sx[i]);
+    }
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_strain_rate(KP p, int begin_step)
+{
+    constexpr int NSTR = ND * (ND + 1) / 2;
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (begin_step && e == 0) {
+        // var.steps++; var.time += var.dt (dynearthsol.cxx:325-326)
+        p.clk->steps += 1;
+        p.clk->time += p.clk->dt;
+    }
+    if (e >= p.ne) return;
+    double s[NSTR];
+    strain_rate_elem<ND>(p, e, s);
+#pragma unroll
+    for (int c = 0; c < NSTR; ++c) p.srate[(size_t)c * p.ne + e] = s[c];
+}
+
+// ==================================================================
+// nodal gathers: heat (fields.cxx:99-146) and dvoldt (geometry.cxx:111-155)
+// ==================================================================
+// contribution of element e to tdot of its local node i
+template <int ND>
+__device__ __forceinline__ double heat_term(const KP &p, int e, int i)
+{
+    constexpr int NPE = ND + 1;
+    double vol = p.vol[e];
+    double kv = m_k(p, e) * vol;
+    double rh = (m_hr(p, e) / m_cp(p, e)) * vol;
+    double sxi = shp_at(p, 0, i, e), szi = shp_at(p, ND - 1, i, e);
+    double syi = (ND == 3) ? shp_at(p, 1, i, e) : 0.0;
+    double diffusion = 0;
+#pragma unroll
+    for (int j = 0; j < NPE; ++j) {
+        double sxj = shp_at(p, 0, j, e), szj = shp_at(p, ND - 1, j, e);
+        double D;
+        if (ND == 3) {
+            double syj = shp_at(p, 1, j, e);
+            D = (sxi * sxj + syi * syj + szi * szj);
+        } else {
+            D = (sxi * sxj + szi * szj);
+        }
+        diffusion += D * p.T[conn_at(p, j, e)];
+    }
+    return diffusion * kv - rh;
+}
+
+template <int ND, bool HEAT, bool DVOLDT>
+__global__ void __launch_bounds__(TPB) k_node_gather1(KP p)
+{
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.nn) return;
+    int b = p.sup_off[n], end = p.sup_off[n + 1];
+    double tdot = 0, dvoldt = 0;
+    for (int q = b; q < end; ++q) {
+        int ent = p.sup_ent[q];
+        int e = ent >> 2, i = ent & 3;
+        if (HEAT) tdot += heat_term<ND>(p, e, i);
+        if (DVOLDT) {
+            double dj;
+            if (ND == 3) dj = p.srate[e] + p.srate[(size_t)p.ne + e] + p.srate[2 * (size_t)p.ne + e];
+            else dj = p.srate[e] + p.srate[(size_t)p.ne + e];
+            dvoldt += dj * p.vol[e];
+        }
+    }
+    if (HEAT) p.tdot[n] = tdot;
+    if (DVOLDT) p.ntmp[n] = dvoldt / p.vol_n[n];
+}
+
+// temperature update + Dirichlet BC (fields.cxx:151-162)
+__global__ void __launch_bounds__(TPB) k_temperature_update(KP p)
+{
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.nn) return;
+    unsigned flag = p.bcflag[n];
+    if (flag & BOUNDZ1) p.T[n] = p.prm.surface_temperature;
+    else if ((flag & BOUNDZ0) && !p.prm.has_fixed_bottom_temperature) p.T[n] = p.prm.mantle_temperature;
+    else p.T[n] -= p.tdot[n] * p.clk->dt / p.tmass[n];
+}
+
+// compute_edvoldt (geometry.cxx:158-179)
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_edvoldt(KP p)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    double dj = 0;
+#pragma unroll
+    for (int i = 0; i < ND + 1; ++i) dj += p.ntmp[conn_at(p, i, e)];
+    p.edvoldt[e] = dj / (ND + 1);
+}
+
+// ==================================================================
+// update_stress (rheology.cxx:510-646)
+// ==================================================================
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_update_stress(KP p, int fused)
+{
+    constexpr int NSTR = ND * (ND + 1) / 2;
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    const size_t ne = p.ne;
+    double edv;
+    if (fused) {
+        // compute_edvoldt fused in: dvoldt of the step is in ntmp
+        double dj = 0;
+#pragma unroll
+        for (int i = 0; i < ND + 1; ++i) dj += p.ntmp[conn_at(p, i, e)];
+        edv = dj / (ND + 1);
+        p.edvoldt[e] = edv;
+    } else {
+        edv = p.edvoldt[e];
+    }
+    double s[NSTR], es[NSTR], edot[NSTR];
+#pragma unroll
+    for (int c = 0; c < NSTR; ++c) {
+        s[c] = p.stress[c * ne + e];
+        es[c] = p.strain[c * ne + e];
+        edot[c] = p.srate[c * ne + e];
+    }
+    double syy = p.syy[e], pls = p.pls[e], dpls = p.dpls[e], dpr;
+    unsigned bits = update_stress_elem<ND>(p, e, p.clk->dt, s, syy, es, edot, pls, dpls, edv, p.vol[e],
+                                           p.vol_old[e], dpr);
+#pragma unroll
+    for (int c = 0; c < NSTR; ++c) {
+        p.stress[c * ne + e] = s[c];
+        p.strain[c * ne + e] = es[c];
+        p.srate[c * ne + e] = edot[c];
+    }
+    p.syy[e] = syy;
+    p.pls[e] = pls;
+    p.dpls[e] = dpls;
+    p.dp[e] = dpr;
+    if (fused && p.rho_e) p.rho_e[e] = m_rho<ND>(p, e);   // temperature is final for this step
+    if (bits) set_err(p, bits);
+}
+
+// ==================================================================
+// NMD_stress (geometry.cxx:182-236)
+// ==================================================================
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_nmd_gather(KP p)
+{
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.nn) return;
+    double acc = 0;
+    for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+        int e = p.sup_ent[q] >> 2;
+        acc += p.dp[e] * p.vol[e];
+    }
+    p.ntmp[n] = acc / p.vol_n[n];
+}
+
+// per-facet force of the gravity-induced stress BCs (bc.cxx:493-557);
+// inactive facets get exactly +0 so that subtracting them is exact
+template <int ND>
+__device__ void facet_force(const KP &p, int q)
+{
+    const int i = p.fac_bdry[q];
+    const int t = p.prm.vbc_types[i];
+    double out[ND];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) out[d] = 0.0;
+    bool active = p.prm.gravity != 0 && (t == 0 || t == 2 || t == 4) &&
+                  !(i == 4 && !p.prm.has_winkler_foundation) && !(i == 5 && !p.prm.has_water_loading);
+    if (active) {
+        const int e = p.fac_elem[q], f = p.fac_f[q];
+        double normal[ND], zcenter;
+        if (ND == 3) {
+            const int F[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
+            double c0[3], c1[3], c2[3];
+            load_node_x<3>(p, conn_at(p, F[f][0], e), c0);
+            load_node_x<3>(p, conn_at(p, F[f][1], e), c1);
+            load_node_x<3>(p, conn_at(p, F[f][2], e), c2);
+            double v01[3], v02[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                v01[d] = c1[d] - c0[d];
+                v02[d] = c2[d] - c0[d];
+            }
+            normal[0] = (v01[1] * v02[2] - v01[2] * v02[1]) / 2;
+            normal[1] = (v01[2] * v02[0] - v01[0] * v02[2]) / 2;
+            normal[ND - 1] = (v01[0] * v02[1] - v01[1] * v02[0]) / 2;
+            zcenter = (c0[2] + c1[2] + c2[2]) / 3;
+        } else {
+            const int F[3][2] = {{1, 2}, {2, 0}, {0, 1}};
+            double c0[2], c1[2];
+            load_node_x<2>(p, conn_at(p, F[f][0], e), c0);
+            load_node_x<2>(p, conn_at(p, F[f][1], e), c1);
+            double v01[2] = {c1[0] - c0[0], c1[1] - c0[1]};
+            normal[0] = v01[1];
+            normal[ND - 1] = -v01[0];
+            zcenter = (c0[1] + c1[1]) / 2;
+        }
+        double pr;
+        if (i == 4 && p.prm.has_winkler_foundation) {
+            double rho = p.rho_e ? p.rho_e[e] : m_rho<ND>(p, e);
+            pr = p.prm.compensation_pressure
+                - (rho + p.prm.winkler_delta_rho) * p.prm.gravity * (zcenter + p.prm.zlength);
+        } else if (i == 5 && p.prm.has_water_loading) {
+            const double sea_level = 0;
+            pr = 0;
+            if (zcenter < sea_level) {
+                const double sea_water_density = 1030;
+                pr = sea_water_density * p.prm.gravity * (sea_level - zcenter);
+            }
+        } else {
+            pr = ref_pressure_(p, zcenter);
+        }
+#pragma unroll
+        for (int d = 0; d < ND; ++d) out[d] = pr * normal[d] / ND;
+    }
+#pragma unroll
+    for (int d = 0; d < ND; ++d) p.fv[(size_t)d * p.nbf + q] = out[d];
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_nmd_correct(KP p, int with_facets)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < p.ne) {
+        const int e = t;
+        double dpn = 0;
+#pragma unroll
+        for (int i = 0; i < ND + 1; ++i) dpn += p.ntmp[conn_at(p, i, e)];
+        double dp_el = dpn / (ND + 1);
+        double dp_orig = p.dp[e];
+#pragma unroll
+        for (int i = 0; i < ND; ++i) p.stress[(size_t)i * p.ne + e] += (-dp_orig + dp_el) / ND;
+    } else if (with_facets && t < p.ne + p.nbf) {
+        facet_force<ND>(p, t - p.ne);
+    }
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_facet_forces(KP p)
+{
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < p.nbf) facet_force<ND>(p, q);
+}
+
+// ==================================================================
+// velocity boundary conditions (bc.cxx:179-490), one node
+// ==================================================================
+template <int ND>
+__device__ __forceinline__ void vbc_x(int type, double val, double *v)
+{
+    switch (type) {
+    case 1: v[0] = val; break;
+    case 2: v[1] = 0; if (ND == 3) v[ND - 1] = 0; break;
+    case 3: v[0] = val; v[1] = 0; if (ND == 3) v[ND - 1] = 0; break;
+    case 4: if (ND == 3) { v[1] = val; v[ND - 1] = 0; } break;
+    case 5: if (ND == 3) { v[0] = 0; v[1] = val; v[ND - 1] = 0; } break;
+    case 7: if (ND == 3) { v[0] = val; v[1] = 0; } break;
+    default: break;
+    }
+}
+
+__device__ __forceinline__ void vbc_y(int type, double val, double *v, bool y1)
+{
+    switch (type) {
+    case 1: v[1] = val; break;
+    case 2: v[0] = 0; v[2] = 0; break;
+    case 3:
+        if (y1) { v[0] = val; v[1] = 0; v[2] = 0; }   // bc.cxx:325-329
+        else { v[0] = 0; v[1] = val; v[2] = 0; }      // bc.cxx:294-298
+        break;
+    case 4: v[0] = val; v[2] = 0; break;
+    case 5: v[0] = val; v[1] = 0; v[2] = 0; break;
+    case 7: v[0] = 0; v[1] = val; break;
+    default: break;
+    }
+}
+
+template <int ND>
+__device__ __forceinline__ void vbc_z(int type, double val, double *v)
+{
+    switch (type) {
+    case 1: v[ND - 1] = val; break;
+    case 2: v[0] = 0; if (ND == 3) v[1] = 0; break;
+    case 3: v[0] = 0; if (ND == 3) v[1] = 0; v[ND - 1] = val; break;
+    default: break;
+    }
+}
+
+template <int ND>
+__device__ void apply_vbcs_node(const KP &p, unsigned flag, double *v)
+{
+    if (!(flag & BOUND_ANY)) return;
+    const int *ty = p.prm.vbc_types;
+    const double *va = p.prm.vbc_values;
+    if (flag & BOUNDX0) vbc_x<ND>(ty[0], va[0], v);
+    if (flag & BOUNDX1) vbc_x<ND>(ty[1], va[1], v);
+    if (ND == 3) {
+        if (flag & BOUNDY0) vbc_y(ty[2], va[2], v, false);
+        if (flag & BOUNDY1) vbc_y(ty[3], va[3], v, true);
+    }
+    for (int ib = 6; ib <= 9; ib++) {
+        if (!(flag & (1u << ib))) continue;
+        const double *n = p.bnormals[ib];
+        double fac = 0;
+        switch (ty[ib]) {
+        case 1:
+            if (flag == (1u << ib)) {
+                double vn = 0;
+                for (int d = 0; d < ND; d++) vn += v[d] * n[d];
+                for (int d = 0; d < ND; d++) v[d] += (va[ib] - vn) * n[d];
+            } else {
+                for (int ic = 0; ic < ib; ic++) {
+                    if (!(flag & (1u << ic))) continue;
+                    if (ty[ic] == 0) {
+                        double vn = 0;
+                        for (int d = 0; d < ND; d++) vn += v[d] * n[d];
+                        for (int d = 0; d < ND; d++) v[d] += (va[ib] - vn) * n[d];
+                    } else if (ty[ic] == 1) {
+                        const double *edge = p.edge_vectors[ic][ib];
+                        double ve = 0;
+                        for (int d = 0; d < ND; d++) ve += v[d] * edge[d];
+                        for (int d = 0; d < ND; d++) v[d] = ve * edge[d];
+                    }
+                }
+            }
+            break;
+        case 3:
+            for (int d = 0; d < ND; d++) v[d] = va[ib] * n[d];
+            break;
+        case 11:
+            fac = 1 / sqrt(1 - n[ND - 1] * n[ND - 1]);
+            if (flag == (1u << ib)) {
+                double vn = 0;
+                for (int d = 0; d < ND - 1; d++) vn += v[d] * n[d];
+                for (int d = 0; d < ND - 1; d++) v[d] += (va[ib] * fac - vn) * n[d];
+            } else {
+                for (int ic = 0; ic < ib; ic++) {
+                    if (!(flag & (1u << ic))) continue;
+                    if (ty[ic] == 0) {
+                        double vn = 0;
+                        for (int d = 0; d < ND - 1; d++) vn += v[d] * n[d];
+                        for (int d = 0; d < ND - 1; d++) v[d] += (va[ib] * fac - vn) * n[d];
+                    } else if (ty[ic] == 1) {
+                        const double *edge = p.edge_vectors[ic][ib];
+                        double ve = 0;
+                        for (int d = 0; d < ND; d++) ve += v[d] * edge[d];
+                        for (int d = 0; d < ND; d++) v[d] = ve * edge[d];
+                    }
+                }
+            }
+            break;
+        case 13:
+            fac = 1 / sqrt(1 - n[ND - 1] * n[ND - 1]);
+            for (int d = 0; d < ND - 1; d++) v[d] = va[ib] * fac * n[d];
+            v[ND - 1] = 0;
+            break;
+        default:
+            break;
+        }
+    }
+    if (ty[4] == 0 && ty[5] == 0) return;
+    if (flag & BOUNDZ0) vbc_z<ND>(ty[4], va[4], v);
+    if (flag & BOUNDZ1) vbc_z<ND>(ty[5], va[5], v);
+}
+
+// ==================================================================
+// update_force (fields.cxx:291-340) with stress BCs (bc.cxx:493-566) and
+// damping (fields.cxx:235-288); optionally fused with update_velocity,
+// apply_vbcs and update_coordinate (dynearthsol.cxx:340-343, fields.cxx:343-368)
+// ==================================================================
+template <int ND>
+__device__ __forceinline__ void damp(const KP &p, double &ff, double v)
+{
+    const double df = p.prm.damping_factor;
+    switch (p.prm.damping_option) {
+    case 1:
+        if (fabs(v) > 1e-13) ff -= df * copysign(ff, v);
+        break;
+    case 2:
+        ff -= df * ff;
+        break;
+    case 3:
+        if ((ff < 0) == (v < 0)) ff -= df * ff;
+        else ff += (1 - df) * ff;
+        break;
+    default:
+        break;
+    }
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
+{
+    constexpr int NSTR = ND * (ND + 1) / 2;
+    constexpr int NPE = ND + 1;
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.nn) return;
+    const size_t ne = p.ne;
+    const double gravity = p.prm.gravity;
+    double f[ND];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) f[d] = 0;
+    for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+        int ent = p.sup_ent[q];
+        int e = ent >> 2, i = ent & 3;
+        double s[NSTR];
+#pragma unroll
+        for (int c = 0; c < NSTR; ++c) s[c] = p.stress[c * ne + e];
+        double vol = p.vol[e];
+        double buoy = 0;
+        if (gravity != 0) {
+            double rho = p.rho_e ? p.rho_e[e] : m_rho<ND>(p, e);
+            buoy = rho * gravity / NPE;
+        }
+        double sx = shp_at(p, 0, i, e), sz = shp_at(p, ND - 1, i, e);
+        if (ND == 3) {
+            double sy = shp_at(p, 1, i, e);
+            f[0] -= (s[0] * sx + s[3] * sy + s[4] * sz) * vol;
+            f[1] -= (s[3] * sx + s[1] * sy + s[5] * sz) * vol;
+            f[ND - 1] -= (s[4] * sx + s[5] * sy + s[2] * sz + buoy) * vol;
+        } else {
+            f[0] -= (s[0] * sx + s[2] * sz) * vol;
+            f[ND - 1] -= (s[2] * sx + s[1] * sz + buoy) * vol;
+        }
+    }
+    // gravity-induced stress BCs, in the reference's facet order
+    for (int q = p.nf_off[n]; q < p.nf_off[n + 1]; ++q) {
+        int fq = p.nf_ent[q];
+#pragma unroll
+        for (int d = 0; d < ND; ++d) f[d] -= p.fv[(size_t)d * p.nbf + fq];
+    }
+    const unsigned flag = p.bcflag[n];
+    if (p.prm.has_elastic_foundation && (flag & BOUNDZ0)) {
+        const size_t o = (size_t)(ND - 1) * p.nn + n;
+        f[ND - 1] -= p.prm.elastic_foundation_constant * (p.x[o] - p.x0[o]);
+    }
+    double v[ND];
+    load_node_v<ND>(p, n, v);
+    if (p.prm.is_quasi_static) {
+#pragma unroll
+        for (int d = 0; d < ND; ++d) damp<ND>(p, f[d], v[d]);
+    }
+#pragma unroll
+    for (int d = 0; d < ND; ++d) p.f[(size_t)d * p.nn + n] = f[d];
+    if (!fused_motion) return;
+    const double dt = p.clk->dt;
+    const double m = p.mass[n];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) v[d] += dt * f[d] / m;
+    apply_vbcs_node<ND>(p, flag, v);
+    bool bad = false;
+#pragma unroll
+    for (int d = 0; d < ND; ++d) {
+        const size_t o = (size_t)d * p.nn + n;
+        p.v[o] = v[d];
+        double xn = p.x[o] + v[d] * dt;
+        p.x[o] = xn;
+        bad |= !isfinite(xn) || !isfinite(v[d]);
+    }
+    if (bad) set_err(p, DES_DEV_NONFINITE);
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_velocity(KP p)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.nn * ND) return;
+    int d = i / p.nn, n = i - d * p.nn;
+    p.v[i] += p.clk->dt * p.f[i] / p.mass[n];
+    (void)d;
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_vbcs(KP p)
+{
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.nn) return;
+    unsigned flag = p.bcflag[n];
+    if (!(flag & BOUND_ANY)) return;
+    double v[ND];
+    load_node_v<ND>(p, n, v);
+    apply_vbcs_node<ND>(p, flag, v);
+#pragma unroll
+    for (int d = 0; d < ND; ++d) p.v[(size_t)d * p.nn + n] = v[d];
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_coordinate(KP p)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.nn * ND) return;
+    p.x[i] += p.v[i] * p.clk->dt;
+}
+
+// ==================================================================
+// element geometry: volume_old swap, compute_volume, compute_shape_fn,
+// rotate_stress, compute_dt element terms
+// ==================================================================
+template <int ND>
+__device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], double vol, double (*shp)[ND + 1])
+{
+    if (ND == 3) {
+        const double *d0 = d[0], *d1 = d[1], *d2 = d[2], *d3 = d[3];
+        double iv = 1 / (6 * vol);
+        double x01 = d0[0] - d1[0], x02 = d0[0] - d2[0], x03 = d0[0] - d3[0];
+        double x12 = d1[0] - d2[0], x13 = d1[0] - d3[0], x23 = d2[0] - d3[0];
+        double y01 = d0[1] - d1[1], y02 = d0[1] - d2[1], y03 = d0[1] - d3[1];
+        double y12 = d1[1] - d2[1], y13 = d1[1] - d3[1], y23 = d2[1] - d3[1];
+        double z01 = d0[2] - d1[2], z02 = d0[2] - d2[2], z03 = d0[2] - d3[2];
+        double z12 = d1[2] - d2[2], z13 = d1[2] - d3[2], z23 = d2[2] - d3[2];
+        shp[0][0] = iv * (y13 * z12 - y12 * z13);
+        shp[0][1] = iv * (y02 * z23 - y23 * z02);
+        shp[0][2] = iv * (y13 * z03 - y03 * z13);
+        shp[0][3] = iv * (y01 * z02 - y02 * z01);
+        shp[1][0] = iv * (z13 * x12 - z12 * x13);
+        shp[1][1] = iv * (z02 * x23 - z23 * x02);
+        shp[1][2] = iv * (z13 * x03 - z03 * x13);
+        shp[1][3] = iv * (z01 * x02 - z02 * x01);
+        shp[ND - 1][0] = iv * (x13 * y12 - x12 * y13);
+        shp[ND - 1][1] = iv * (x02 * y23 - x23 * y02);
+        shp[ND - 1][2] = iv * (x13 * y03 - x03 * y13);
+        shp[ND - 1][3] = iv * (x01 * y02 - x02 * y01);
+    } else {
+        const double *d0 = d[0], *d1 = d[1], *d2 = d[2];
+        double iv = 1 / (2 * vol);
+        shp[0][0] = iv * (d1[1] - d2[1]);
+        shp[0][1] = iv * (d2[1] - d0[1]);
+        shp[0][2] = iv * (d0[1] - d1[1]);
+        shp[ND - 1][0] = iv * (d2[0] - d1[0]);
+        shp[ND - 1][1] = iv * (d0[0] - d2[0]);
+        shp[ND - 1][2] = iv * (d1[0] - d0[0]);
+    }
+}
+
+// jaumann_rate_3d / _2d (fields.cxx:375-404)
+__device__ __forceinline__ void jaumann3(double *s, double dt, double w3, double w4, double w5)
+{
+    double si[6];
+    si[0] = -2.0 * s[3] * w3 - 2.0 * s[4] * w4;
+    si[1] = 2.0 * s[3] * w3 - 2.0 * s[5] * w5;
+    si[2] = 2.0 * s[4] * w4 + 2.0 * s[5] * w5;
+    si[3] = s[0] * w3 - s[1] * w3 - s[4] * w5 - s[5] * w4;
+    si[4] = s[0] * w4 - s[2] * w4 + s[3] * w5 - s[5] * w3;
+    si[5] = s[1] * w5 - s[2] * w5 + s[3] * w4 + s[4] * w3;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s[i] += dt * si[i];
+}
+
+__device__ __forceinline__ void jaumann2(double *s, double dt, double w2)
+{
+    double si[3];
+    si[0] = -2.0 * s[2] * w2;
+    si[1] = 2.0 * s[2] * w2;
+    si[2] = s[0] * w2 - s[1] * w2;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) s[i] += dt * si[i];
+}
+
+template <int ND>
+__device__ __forceinline__ void warp_block_min(unsigned long long val, unsigned long long *target)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long other = __shfl_xor_sync(0xffffffffu, val, o);
+        val = other < val ? other : val;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMin(target, val);
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
+{
+    constexpr int NSTR = ND * (ND + 1) / 2;
+    constexpr int NPE = ND + 1;
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = e < p.ne;
+    const size_t ne = p.ne;
+    bool do_dt = (flags & GEO_DT) != 0;
+    if (flags & GEO_DT_IF_STEP) do_dt = do_dt && (p.clk->steps % 10 == 0);
+    do_dt = do_dt && p.prm.fixed_dt == 0;
+    unsigned long long b_minh = ~0ull, b_maxwell = ~0ull, b_diff = ~0ull;
+    if (in) {
+        double c[NPE][ND];
+        int nodes[NPE];
+#pragma unroll
+        for (int i = 0; i < NPE; ++i) {
+            nodes[i] = conn_at(p, i, e);
+            load_node_x<ND>(p, nodes[i], c[i]);
+        }
+        double vol;
+        if (flags & GEO_COPY_OLD) p.vol_old[e] = p.vol[e];
+        if (flags & GEO_VOLUME) {
+            if (ND == 3) vol = tet_volume(c[0], c[1], c[2], c[NPE - 1]);
+            else vol = tri_area<2>(c[0], c[1], c[2]);
+            p.vol[e] = vol;
+            if (!(vol > 0)) set_err(p, DES_DEV_NEG_VOLUME);
+        } else {
+            vol = p.vol[e];
+        }
+        double shp[ND][NPE];
+        if (flags & GEO_SHAPE) {
+            shape_fn_elem<ND>(c, vol, shp);
+#pragma unroll
+            for (int k = 0; k < ND; ++k)
+#pragma unroll
+                for (int i = 0; i < NPE; ++i) p.shp[((size_t)k * NPE + i) * ne + e] = shp[k][i];
+        } else if (flags & GEO_ROTATE) {
+#pragma unroll
+            for (int k = 0; k < ND; ++k)
+#pragma unroll
+                for (int i = 0; i < NPE; ++i) shp[k][i] = p.shp[((size_t)k * NPE + i) * ne + e];
+        }
+        if (flags & GEO_ROTATE) {
+            double v[NPE][ND];
+#pragma unroll
+            for (int i = 0; i < NPE; ++i) load_node_v<ND>(p, nodes[i], v[i]);
+            const double dt = p.clk->dt;
+            double s[NSTR], es[NSTR];
+#pragma unroll
+            for (int cc = 0; cc < NSTR; ++cc) {
+                s[cc] = p.stress[cc * ne + e];
+                es[cc] = p.strain[cc * ne + e];
+            }
+            if (ND == 3) {
+                double w3 = 0, w4 = 0, w5 = 0;
+#pragma unroll
+                for (int i = 0; i < NPE; ++i) w3 += 0.5 * (v[i][0] * shp[1][i] - v[i][1] * shp[0][i]);
+#pragma unroll
+                for (int i = 0; i < NPE; ++i) w4 += 0.5 * (v[i][0] * shp[ND - 1][i] - v[i][ND - 1] * shp[0][i]);
+#pragma unroll
+                for (int i = 0; i < NPE; ++i) w5 += 0.5 * (v[i][1] * shp[ND - 1][i] - v[i][ND - 1] * shp[1][i]);
+                jaumann3(s, dt, w3, w4, w5);
+                jaumann3(es, dt, w3, w4, w5);
+            } else {
+                double w2 = 0;
+#pragma unroll
+                for (int i = 0; i < NPE; ++i) w2 += 0.5 * (v[i][ND - 1] * shp[0][i] - v[i][0] * shp[ND - 1][i]);
+                jaumann2(s, dt, w2);
+                jaumann2(es, dt, w2);
+            }
+#pragma unroll
+            for (int cc = 0; cc < NSTR; ++cc) {
+                p.stress[cc * ne + e] = s[cc];
+                p.strain[cc * ne + e] = es[cc];
+            }
+        }
+        if (do_dt) {
+            // compute_dt element terms (geometry.cxx:254-292)
+            double minh;
+            if (ND == 3) {
+                double maxa = dmax_(dmax_(tri_area<3>(c[0], c[1], c[2]), tri_area<3>(c[0], c[1], c[NPE - 1])),
+                                    dmax_(tri_area<3>(c[2], c[NPE - 1], c[0]),
+                                          tri_area<3>(c[2], c[NPE - 1], c[1])));
+                minh = 3 * vol / maxa;
+            } else {
+                double d01 = 0, d12 = 0, d02 = 0;
+#pragma unroll
+                for (int k = 0; k < ND; ++k) {
+                    double a = c[1][k] - c[0][k], b = c[2][k] - c[1][k], cc = c[2][k] - c[0][k];
+                    d01 += a * a;
+                    d12 += b * b;
+                    d02 += cc * cc;
+                }
+                double maxl = sqrt(dmax_(dmax_(d01, d12), d02));
+                minh = 2 * vol / maxl;
+            }
+            double tmax = 0.5 * p.mat.visc_min / (1e-40 + m_shearm(p, e));
+            b_minh = dbits(minh);
+            b_maxwell = dbits(tmax);
+            if (p.prm.has_thermal_diffusion) b_diff = dbits(0.5 * minh * minh / p.mat.therm_diff_max);
+        }
+    }
+    if (do_dt) {   // uniform across the grid: every thread reaches the shuffles
+        warp_block_min<ND>(b_minh, &p.clk->red_minh);
+        warp_block_min<ND>(b_maxwell, &p.clk->red_maxwell);
+        warp_block_min<ND>(b_diff, &p.clk->red_diffusion);
+    }
+}
+
+// compute_dt final combination (geometry.cxx:294-309), single thread
+template <int ND>
+__global__ void k_dt_finalize(KP p, int only_on_step)
+{
+    Clock *ck = p.clk;
+    if (only_on_step && ck->steps % 10 != 0) return;
+    double dt;
+    if (p.prm.fixed_dt != 0) {
+        dt = p.prm.fixed_dt;
+    } else {
+        double minl = bitsd(ck->red_minh);
+        double dt_maxwell = ck->red_maxwell == ~0ull ? DBL_MAX : bitsd(ck->red_maxwell);
+        double dt_diffusion = ck->red_diffusion == ~0ull ? DBL_MAX : bitsd(ck->red_diffusion);
+        if (ck->red_minh == ~0ull) minl = DBL_MAX;
+        double dt_advection = 0.5 * minl / p.prm.max_vbc_val;
+        double dt_elastic = p.prm.is_quasi_static
+            ? 0.5 * minl / (p.prm.max_vbc_val * p.prm.inertial_scaling)
+            : 0.5 * minl / sqrt(m_bulkm(p, 0) / m_rho<ND>(p, 0));
+        dt = dmin_(dmin_(dt_elastic, dt_maxwell), dmin_(dt_advection, dt_diffusion)) * p.prm.dt_fraction;
+        ck->last_dt_terms[0] = dt_maxwell;
+        ck->last_dt_terms[1] = dt_diffusion;
+        ck->last_dt_terms[2] = dt_advection;
+        ck->last_dt_terms[3] = dt_elastic;
+        if (dt <= 0) atomicOr(p.err, 0x100u);   // reported as DES_ERUNTIME
+    }
+    ck->dt = dt;
+    ck->red_minh = ck->red_maxwell = ck->red_diffusion = ~0ull;
+}
+
+__global__ void k_dt_reset(KP p)
+{
+    p.clk->red_minh = p.clk->red_maxwell = p.clk->red_diffusion = ~0ull;
+}
+
+// ==================================================================
+// compute_mass (geometry.cxx:313-365)
+// ==================================================================
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_mass(KP p)
+{
+    constexpr int NPE = ND + 1;
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.nn) return;
+    const double pseudo_speed = p.prm.max_vbc_val * p.prm.inertial_scaling;
+    const bool quasi = p.prm.is_quasi_static, thermal = p.prm.has_thermal_diffusion;
+    double vn = 0, ms = 0, tm = 0;
+    for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+        int e = p.sup_ent[q] >> 2;
+        double vol = p.vol[e];
+        double rho_e = p.rho_e ? p.rho_e[e] : m_rho<ND>(p, e);
+        double rho = quasi ? m_bulkm(p, e) / (pseudo_speed * pseudo_speed) : rho_e;
+        double m = rho * vol / NPE;
+        vn += vol;
+        ms += m;
+        if (thermal) tm += rho_e * m_cp(p, e) * vol / NPE;
+    }
+    p.vol_n[n] = vn;
+    p.mass[n] = ms;
+    p.tmass[n] = tm;
+}
+
+// ==================================================================
+// worst element quality (geometry.cxx:458-512)
+// ==================================================================
+template <int ND>
+__device__ __forceinline__ double elem_quality(const KP &p, int e)
+{
+    constexpr int NPE = ND + 1;
+    double c[NPE][ND];
+#pragma unroll
+    for (int i = 0; i < NPE; ++i) load_node_x<ND>(p, conn_at(p, i, e), c[i]);
+    double vol = p.vol[e];
+    if (ND == 3) {
+        double normalization_factor = 216 * sqrt(3.0);
+        double area_sum = (tri_area<3>(c[0], c[1], c[2]) + tri_area<3>(c[0], c[1], c[NPE - 1])
+                           + tri_area<3>(c[2], c[NPE - 1], c[0]) + tri_area<3>(c[2], c[NPE - 1], c[1]));
+        return normalization_factor * vol * vol / (area_sum * area_sum * area_sum);
+    }
+    double normalization_factor = 4 * sqrt(3.0);
+    double d01 = 0, d12 = 0, d02 = 0;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+        double a = c[1][k] - c[0][k], b = c[2][k] - c[1][k], cc = c[2][k] - c[0][k];
+        d01 += a * a;
+        d12 += b * b;
+        d02 += cc * cc;
+    }
+    double dist2_sum = d01 + d12 + d02;
+    return normalization_factor * vol / dist2_sum;
+}
+
+// red[0] = min quality bits (quality > 0), red[1] = smallest index at that minimum
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_quality_min(KP p, unsigned long long *red)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long b = ~0ull;
+    if (e < p.ne) {
+        double q = elem_quality<ND>(p, e);
+        b = q > 0 ? dbits(q) : 0ull;
+    }
+    warp_block_min<ND>(b, &red[0]);
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_quality_arg(KP p, unsigned long long *red)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    double q = elem_quality<ND>(p, e);
+    unsigned long long b = q > 0 ? dbits(q) : 0ull;
+    if (b == red[0]) atomicMin(&red[1], (unsigned long long)e);
+}
+
+// ==================================================================
+// AoS <-> SoA
+// ==================================================================
+__global__ void k_aos_to_soa(const double *__restrict__ aos, double *__restrict__ soa, int n, int nc)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)n * nc) return;
+    long long r = i / nc, c = i - r * nc;
+    soa[c * n + r] = aos[i];
+}
+
+__global__ void k_soa_to_aos(const double *__restrict__ soa, double *__restrict__ aos, int n, int nc)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)n * nc) return;
+    long long r = i / nc, c = i - r * nc;
+    aos[i] = soa[c * n + r];
+}
+
+// ==================================================================
+// launchers
+// ==================================================================
+#define DISPATCH(KERNEL, GRID, ...)                                       \
+    do {                                                                  \
+        if (p.nd == 3) KERNEL<3><<<(GRID), TPB, 0, s>>>(__VA_ARGS__);     \
+        else KERNEL<2><<<(GRID), TPB, 0, s>>>(__VA_ARGS__);               \
+    } while (0)
+
+int launch_strain_rate(const KP &p, cudaStream_t s, bool begin_step)
+{
+    DISPATCH(k_strain_rate, nblocks(p.ne), p, (int)begin_step);
+    return 1;
+}
+
+int launch_heat_gather(const KP &p, cudaStream_t s)
+{
+    if (p.nd == 3) k_node_gather1<3, true, false><<<nblocks(p.nn), TPB, 0, s>>>(p);
+    else k_node_gather1<2, true, false><<<nblocks(p.nn), TPB, 0, s>>>(p);
+    return 1;
+}
+
+int launch_dvoldt(const KP &p, cudaStream_t s)
+{
+    if (p.nd == 3) k_node_gather1<3, false, true><<<nblocks(p.nn), TPB, 0, s>>>(p);
+    else k_node_gather1<2, false, true><<<nblocks(p.nn), TPB, 0, s>>>(p);
+    return 1;
+}
+
+int launch_heat_and_dvoldt(const KP &p, cudaStream_t s)
+{
+    if (p.nd == 3) k_node_gather1<3, true, true><<<nblocks(p.nn), TPB, 0, s>>>(p);
+    else k_node_gather1<2, true, true><<<nblocks(p.nn), TPB, 0, s>>>(p);
+    return 1;
+}
+
+int launch_temperature_update(const KP &p, cudaStream_t s)
+{
+    k_temperature_update<<<nblocks(p.nn), TPB, 0, s>>>(p);
+    return 1;
+}
+
+int launch_edvoldt(const KP &p, cudaStream_t s)
+{
+    DISPATCH(k_edvoldt, nblocks(p.ne), p);
+    return 1;
+}
+
+int launch_update_stress(const KP &p, cudaStream_t s, bool fused)
+{
+    DISPATCH(k_update_stress, nblocks(p.ne), p, (int)fused);
+    return 1;
+}
+
+int launch_nmd_gather(const KP &p, cudaStream_t s)
+{
+    DISPATCH(k_nmd_gather, nblocks(p.nn), p);
+    return 1;
+}
+
+int launch_nmd_correct(const KP &p, cudaStream_t s, bool with_facets)
+{
+    long long n = p.ne + (with_facets ? p.nbf : 0);
+    DISPATCH(k_nmd_correct, nblocks(n), p, (int)with_facets);
+    return 1;
+}
+
+int launch_facet_forces(const KP &p, cudaStream_t s)
+{
+    if (p.nbf == 0) return 0;
+    DISPATCH(k_facet_forces, nblocks(p.nbf), p);
+    return 1;
+}
+
+int launch_force(const KP &p, cudaStream_t s, bool fused_motion)
+{
+    DISPATCH(k_force, nblocks(p.nn), p, (int)fused_motion);
+    return 1;
+}
+
+int launch_velocity(const KP &p, cudaStream_t s)
+{
+    DISPATCH(k_velocity, nblocks((long long)p.nn * p.nd), p);
+    return 1;
+}
+
+int launch_vbcs(const KP &p, cudaStream_t s)
+{
+    DISPATCH(k_vbcs, nblocks(p.nn), p);
+    return 1;
+}
+
+int launch_coordinate(const KP &p, cudaStream_t s)
+{
+    DISPATCH(k_coordinate, nblocks((long long)p.nn * p.nd), p);
+    return 1;
+}
+
+int launch_geometry(const KP &p, cudaStream_t s, int flags)
+{
+    DISPATCH(k_geometry, nblocks(p.ne), p, flags);
+    return 1;
+}
+
+int launch_mass(const KP &p, cudaStream_t s)
+{
+    DISPATCH(k_mass, nblocks(p.nn), p);
+    return 1;
+}
+
+int launch_dt_finalize(const KP &p, cudaStream_t s, bool only_on_step)
+{
+    if (p.nd == 3) k_dt_finalize<3><<<1, 1, 0, s>>>(p, (int)only_on_step);
+    else k_dt_finalize<2><<<1, 1, 0, s>>>(p, (int)only_on_step);
+    return 1;
+}
+
+int launch_dt_reset(const KP &p, cudaStream_t s)
+{
+    k_dt_reset<<<1, 1, 0, s>>>(p);
+    return 1;
+}
+
+int launch_quality(const KP &p, cudaStream_t s, unsigned long long *red)
+{
+    DISPATCH(k_quality_min, nblocks(p.ne), p, red);
+    DISPATCH(k_quality_arg, nblocks(p.ne), p, red);
+    return 2;
+}
+
+int launch_aos_to_soa(const double *aos, double *soa, int n, int ncomp, cudaStream_t s)
+{
+    k_aos_to_soa<<<nblocks((long long)n * ncomp), TPB, 0, s>>>(aos, soa, n, ncomp);
+    return 1;
+}
+
+int launch_soa_to_aos(const double *soa, double *aos, int n, int ncomp, cudaStream_t s)
+{
+    k_soa_to_aos<<<nblocks((long long)n * ncomp), TPB, 0, s>>>(soa, aos, n, ncomp);
+    return 1;
+}
+
+}  // namespace des

@@ -1,0 +1,45 @@
+// des_kernels.cuh -- host-side launchers of the explicit-step kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "des_common.cuh"
+
+namespace des {
+
+// flags of the element geometry pass
+enum GeoFlags : int {
+    GEO_COPY_OLD = 1,    // volume_old <- volume        (dynearthsol.cxx:226)
+    GEO_VOLUME = 2,      // compute_volume              (geometry.cxx:86-108)
+    GEO_SHAPE = 4,       // compute_shape_fn            (geometry.cxx:368-455)
+    GEO_ROTATE = 8,      // rotate_stress               (fields.cxx:411-483)
+    GEO_DT = 16,         // compute_dt element terms    (geometry.cxx:254-292)
+    GEO_DT_IF_STEP = 32  // ... only when steps % 10 == 0 (dynearthsol.cxx:349-361)
+};
+
+// Each launcher returns the number of kernels it launched.
+int launch_strain_rate(const KP &p, cudaStream_t s, bool begin_step);
+int launch_heat_gather(const KP &p, cudaStream_t s);              // tdot -> p.tdot
+int launch_temperature_update(const KP &p, cudaStream_t s);       // T from p.tdot
+int launch_dvoldt(const KP &p, cudaStream_t s);                   // -> ntmp
+int launch_heat_and_dvoldt(const KP &p, cudaStream_t s);          // fused: tdot -> p.tdot, dvoldt -> ntmp
+int launch_edvoldt(const KP &p, cudaStream_t s);
+int launch_update_stress(const KP &p, cudaStream_t s, bool fused);
+int launch_nmd_gather(const KP &p, cudaStream_t s);               // dp_nd -> ntmp
+int launch_nmd_correct(const KP &p, cudaStream_t s, bool with_facets);
+int launch_facet_forces(const KP &p, cudaStream_t s);
+int launch_force(const KP &p, cudaStream_t s, bool fused_motion);
+int launch_velocity(const KP &p, cudaStream_t s);
+int launch_vbcs(const KP &p, cudaStream_t s);
+int launch_coordinate(const KP &p, cudaStream_t s);
+int launch_geometry(const KP &p, cudaStream_t s, int flags);
+int launch_mass(const KP &p, cudaStream_t s);
+int launch_dt_finalize(const KP &p, cudaStream_t s, bool only_on_step);
+int launch_quality(const KP &p, cudaStream_t s, unsigned long long *red);
+int launch_dt_reset(const KP &p, cudaStream_t s);
+
+// layout conversion between the reference's AoS rows and device SoA
+int launch_aos_to_soa(const double *aos, double *soa, int n, int ncomp, cudaStream_t s);
+int launch_soa_to_aos(const double *soa, double *aos, int n, int ncomp, cudaStream_t s);
+
+}  // namespace des

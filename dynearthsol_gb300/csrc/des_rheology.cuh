@@ -1,0 +1,499 @@
+// des_rheology.cuh -- per-element constitutive update (update_stress,
+// rheology.cxx:510-646) and the 3x3 symmetric eigen-solver it needs.
+//
+// The eigen-solver is the hybrid method of J. Kopp, "Efficient numerical
+// diagonalization of hermitian 3x3 matrices", Int. J. Mod. Phys. C 19 (2008)
+// 523 (arXiv:physics/0610206), which the reference vendors as 3x3-C/dsyevh3.c:
+// analytic (Cardano) eigenvalues, eigenvectors from cross products, and a
+// Householder + QL fallback when a cross product is too small.  The branch
+// criterion and the arithmetic order are kept as there, so that FP64 runs
+// take the same branches as the reference.  Only the upper triangle of A is
+// read.  The QL loop keeps the published 30-sweep cap; hitting it sets
+// DES_DEV_QL_NOCONV instead of returning an unchecked -1.
+#pragma once
+
+#include "des_common.cuh"
+
+namespace des {
+
+__device__ __forceinline__ void eig_cardano(const double A[3][3], double w[3])
+{
+    const double inv_sqrt3 = 1.0 / 1.73205080756887729352744634151;
+    double de = A[0][1] * A[1][2];
+    double dd = A[0][1] * A[0][1];
+    double ee = A[1][2] * A[1][2];
+    double ff = A[0][2] * A[0][2];
+    double m = A[0][0] + A[1][1] + A[2][2];
+    double c1 = (A[0][0] * A[1][1] + A[0][0] * A[2][2] + A[1][1] * A[2][2]) - (dd + ee + ff);
+    double c0 = A[2][2] * dd + A[0][0] * ee + A[1][1] * ff - A[0][0] * A[1][1] * A[2][2]
+        - 2.0 * A[0][2] * de;
+    double p = m * m - 3.0 * c1;
+    double q = m * (p - (3.0 / 2.0) * c1) - (27.0 / 2.0) * c0;
+    double sqrt_p = sqrt(fabs(p));
+    double phi = 27.0 * (0.25 * (c1 * c1) * (p - c1) + c0 * (q + 27.0 / 4.0 * c0));
+    phi = (1.0 / 3.0) * atan2(sqrt(fabs(phi)), q);
+    double cc = sqrt_p * cos(phi);
+    double ss = inv_sqrt3 * sqrt_p * sin(phi);
+    double mid = (1.0 / 3.0) * (m - cc);
+    w[2] = mid + ss;
+    w[0] = mid + cc;
+    w[1] = mid - ss;
+}
+
+__device__ __forceinline__ void eig_tridiag(const double A[3][3], double Q[3][3], double d[3], double e[3])
+{
+    double u[3], q[3];
+    double omega, f, K, h, g;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        Q[i][i] = 1.0;
+#pragma unroll
+        for (int j = 0; j < i; j++) Q[i][j] = Q[j][i] = 0.0;
+    }
+    h = A[0][1] * A[0][1] + A[0][2] * A[0][2];
+    g = (A[0][1] > 0) ? -sqrt(h) : sqrt(h);
+    e[0] = g;
+    f = g * A[0][1];
+    u[1] = A[0][1] - g;
+    u[2] = A[0][2];
+    omega = h - f;
+    if (omega > 0.0) {
+        omega = 1.0 / omega;
+        K = 0.0;
+#pragma unroll
+        for (int i = 1; i < 3; i++) {
+            f = A[1][i] * u[1] + A[i][2] * u[2];
+            q[i] = omega * f;
+            K += u[i] * f;
+        }
+        K *= 0.5 * (omega * omega);
+#pragma unroll
+        for (int i = 1; i < 3; i++) q[i] = q[i] - K * u[i];
+        d[0] = A[0][0];
+        d[1] = A[1][1] - 2.0 * q[1] * u[1];
+        d[2] = A[2][2] - 2.0 * q[2] * u[2];
+#pragma unroll
+        for (int j = 1; j < 3; j++) {
+            f = omega * u[j];
+#pragma unroll
+            for (int i = 1; i < 3; i++) Q[i][j] = Q[i][j] - f * u[i];
+        }
+        e[1] = A[1][2] - q[1] * u[2] - u[1] * q[2];
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; i++) d[i] = A[i][i];
+        e[1] = A[1][2];
+    }
+}
+
+// returns 0, or -1 when a 30-sweep cap is hit
+__device__ inline int eig_ql(const double A[3][3], double Q[3][3], double w[3])
+{
+    double e[3];
+    double g, r, p, f, b, s, c, t;
+    int m;
+    eig_tridiag(A, Q, w, e);
+    for (int l = 0; l < 2; l++) {
+        int sweeps = 0;
+        for (;;) {
+            for (m = l; m <= 1; m++) {
+                g = fabs(w[m]) + fabs(w[m + 1]);
+                if (fabs(e[m]) + g == g) break;
+            }
+            if (m == l) break;
+            if (sweeps++ >= 30) return -1;
+            g = (w[l + 1] - w[l]) / (e[l] + e[l]);
+            r = sqrt(g * g + 1.0);
+            if (g > 0) g = w[m] - w[l] + e[l] / (g + r);
+            else g = w[m] - w[l] + e[l] / (g - r);
+            s = c = 1.0;
+            p = 0.0;
+            for (int i = m - 1; i >= l; i--) {
+                f = s * e[i];
+                b = c * e[i];
+                if (fabs(f) > fabs(g)) {
+                    c = g / f;
+                    r = sqrt(c * c + 1.0);
+                    e[i + 1] = f * r;
+                    c *= (s = 1.0 / r);
+                } else {
+                    s = f / g;
+                    r = sqrt(s * s + 1.0);
+                    e[i + 1] = g * r;
+                    s *= (c = 1.0 / r);
+                }
+                g = w[i + 1] - p;
+                r = (w[i] - g) * s + 2.0 * c * b;
+                p = s * r;
+                w[i + 1] = g + p;
+                g = c * r - b;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    t = Q[k][i + 1];
+                    Q[k][i + 1] = s * Q[k][i] + c * t;
+                    Q[k][i] = c * Q[k][i] - s * t;
+                }
+            }
+            w[l] -= p;
+            e[l] = g;
+            e[m] = 0.0;
+        }
+    }
+    return 0;
+}
+
+__device__ inline int eig_hybrid(const double A[3][3], double Q[3][3], double w[3])
+{
+    double norm, error, t, u;
+    eig_cardano(A, w);
+    t = fabs(w[0]);
+    if ((u = fabs(w[1])) > t) t = u;
+    if ((u = fabs(w[2])) > t) t = u;
+    if (t < 1.0) u = t;
+    else u = t * t;
+    error = 256.0 * DBL_EPSILON * (u * u);
+
+    Q[0][1] = A[0][1] * A[1][2] - A[0][2] * A[1][1];
+    Q[1][1] = A[0][2] * A[0][1] - A[1][2] * A[0][0];
+    Q[2][1] = A[0][1] * A[0][1];
+
+    Q[0][0] = Q[0][1] + A[0][2] * w[0];
+    Q[1][0] = Q[1][1] + A[1][2] * w[0];
+    Q[2][0] = (A[0][0] - w[0]) * (A[1][1] - w[0]) - Q[2][1];
+    norm = Q[0][0] * Q[0][0] + Q[1][0] * Q[1][0] + Q[2][0] * Q[2][0];
+    if (norm <= error) return eig_ql(A, Q, w);
+    norm = sqrt(1.0 / norm);
+#pragma unroll
+    for (int j = 0; j < 3; j++) Q[j][0] = Q[j][0] * norm;
+
+    Q[0][1] = Q[0][1] + A[0][2] * w[1];
+    Q[1][1] = Q[1][1] + A[1][2] * w[1];
+    Q[2][1] = (A[0][0] - w[1]) * (A[1][1] - w[1]) - Q[2][1];
+    norm = Q[0][1] * Q[0][1] + Q[1][1] * Q[1][1] + Q[2][1] * Q[2][1];
+    if (norm <= error) return eig_ql(A, Q, w);
+    norm = sqrt(1.0 / norm);
+#pragma unroll
+    for (int j = 0; j < 3; j++) Q[j][1] = Q[j][1] * norm;
+
+    Q[0][2] = Q[1][0] * Q[2][1] - Q[2][0] * Q[1][1];
+    Q[1][2] = Q[2][0] * Q[0][1] - Q[0][0] * Q[2][1];
+    Q[2][2] = Q[0][0] * Q[1][1] - Q[1][0] * Q[0][1];
+    return 0;
+}
+
+// principal_stresses3 (rheology.cxx:13-68)
+__device__ __forceinline__ int principal_stresses3(const double *s, double p[3], double v[3][3])
+{
+    double a[3][3];
+    a[0][0] = s[0];
+    a[1][1] = s[1];
+    a[2][2] = s[2];
+    a[0][1] = s[3];
+    a[0][2] = s[4];
+    a[1][2] = s[5];
+    a[1][0] = a[2][0] = a[2][1] = 0;
+    int rc = eig_hybrid(a, v, p);
+    // compare-and-swap on (0,1), (1,2), (0,1)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int i = (k == 1) ? 1 : 0, j = i + 1;
+        if (p[i] > p[j]) {
+            double t = p[i];
+            p[i] = p[j];
+            p[j] = t;
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+                double b = v[r][i];
+                v[r][i] = v[r][j];
+                v[r][j] = b;
+            }
+        }
+    }
+    return rc;
+}
+
+// principal_stresses2 (rheology.cxx:71-102)
+__device__ __forceinline__ void principal_stresses2(const double *s, double p[2], double &cos2t, double &sin2t)
+{
+    double s0 = 0.5 * (s[0] + s[1]);
+    double rad = second_invariant_<2>(s);
+    p[0] = s0 - rad;
+    p[1] = s0 + rad;
+    const double eps = 1e-15;
+    double a = 0.5 * (s[0] - s[1]);
+    double b = -rad;
+    if (b < -eps) {
+        cos2t = a / b;
+        sin2t = s[2] / b;
+    } else {
+        cos2t = 1;
+        sin2t = 0;
+    }
+}
+
+// elastic (rheology.cxx:105-115)
+template <int ND>
+__device__ __forceinline__ void elastic_(double bulkm, double shearm, const double *de, double *s)
+{
+    constexpr int NSTR = ND * (ND + 1) / 2;
+    double lambda = bulkm - 2. / 3 * shearm;
+    double dev = trace_<ND>(de);
+#pragma unroll
+    for (int i = 0; i < ND; ++i) s[i] += 2 * shearm * de[i] + lambda * dev;
+#pragma unroll
+    for (int i = ND; i < NSTR; ++i) s[i] += 2 * shearm * de[i];
+}
+
+// maxwell (rheology.cxx:118-134)
+template <int ND>
+__device__ __forceinline__ void maxwell_(double bulkm, double shearm, double viscosity, double dt,
+                                         double dv, const double *de, double *s)
+{
+    constexpr int NSTR = ND * (ND + 1) / 2;
+    double tmp = 0.5 * dt * shearm / viscosity;
+    double f1 = 1 - tmp;
+    double f2 = 1 / (1 + tmp);
+    double dev = trace_<ND>(de) / ND;
+    double s0 = trace_<ND>(s) / ND;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) s[i] = ((s[i] - s0) * f1 + 2 * shearm * (de[i] - dev)) * f2 + s0 + bulkm * dv;
+#pragma unroll
+    for (int i = ND; i < NSTR; ++i) s[i] = (s[i] * f1 + 2 * shearm * de[i]) * f2;
+}
+
+// viscous (rheology.cxx:137-148)
+template <int ND>
+__device__ __forceinline__ void viscous_(double bulkm, double viscosity, double total_dv, const double *edot,
+                                         double *s)
+{
+    constexpr int NSTR = ND * (ND + 1) / 2;
+    double dev = trace_<ND>(edot) / ND;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) s[i] = 2 * viscosity * (edot[i] - dev) + bulkm * total_dv;
+#pragma unroll
+    for (int i = ND; i < NSTR; ++i) s[i] = 2 * viscosity * edot[i];
+}
+
+// elasto_plastic: Mohr-Coulomb return map in principal space (rheology.cxx:151-299)
+template <int ND>
+__device__ int elasto_plastic_(double bulkm, double shearm, double amc, double anphi, double anpsi,
+                               double hardn, double ten_max, const double *de, double &depls, double *s)
+{
+    elastic_<ND>(bulkm, shearm, de, s);
+    depls = 0;
+    double p[3];
+    double v[3][3];
+    double cos2t = 1, sin2t = 0;
+    int rc = 0;
+    if (ND == 3) rc = principal_stresses3(s, p, v);
+    else principal_stresses2(s, p, cos2t, sin2t);
+    constexpr int last = ND - 1;
+    double fs = p[0] - p[last] * anphi + amc;
+    double ft = p[last] - ten_max;
+    if (fs > 0 && ft < 0) return rc;
+
+    double pa = sqrt(1 + anphi * anphi) + anphi;
+    double ps = ten_max * anphi - amc;
+    double h = p[last] - ten_max + pa * (p[0] - ps);
+    double a1 = bulkm + 4. / 3 * shearm;
+    double a2 = bulkm - 2. / 3 * shearm;
+    double alam;
+    if (h < 0) {
+        alam = fs / (a1 - a2 * anpsi + a1 * anphi * anpsi - a2 * anphi + 2 * sqrt(anphi) * hardn);
+        p[0] -= alam * (a1 - a2 * anpsi);
+        if (ND == 3) p[1] -= alam * (a2 - a2 * anpsi);
+        p[last] -= alam * (a2 - a1 * anpsi);
+        if (ND == 3) depls = fabs(alam) * sqrt((7 + 4 * anpsi + 7 * anpsi * anpsi) / 18);
+        else depls = fabs(alam) * sqrt((3 + 2 * anpsi + 3 * anpsi * anpsi) / 8);
+    } else {
+        alam = ft / a1;
+        p[0] -= alam * a2;
+        if (ND == 3) p[1] -= alam * a2;
+        p[last] -= alam * a1;
+        if (ND == 3) depls = fabs(alam) * sqrt(7. / 18);
+        else depls = fabs(alam) * sqrt(3. / 8);
+    }
+    if (ND == 3) {
+        double ss[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+        for (int m = 0; m < 3; m++)
+#pragma unroll
+            for (int n = m; n < 3; n++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) ss[m][n] += v[m][k] * v[n][k] * p[k];
+        s[0] = ss[0][0];
+        s[1] = ss[1][1];
+        s[2] = ss[2][2];
+        s[3] = ss[0][1];
+        s[4] = ss[0][2];
+        s[5] = ss[1][2];
+    } else {
+        double dc2 = (p[0] - p[1]) * cos2t;
+        double dss = p[0] + p[1];
+        s[0] = 0.5 * (dss + dc2);
+        s[1] = 0.5 * (dss - dc2);
+        s[2] = 0.5 * (p[0] - p[1]) * sin2t;
+    }
+    return rc;
+}
+
+// elasto_plastic2d: plane-strain Mohr-Coulomb (rheology.cxx:302-507)
+__device__ inline void elasto_plastic2d_(double bulkm, double shearm, double amc, double anphi, double anpsi,
+                                  double hardn, double ten_max, const double *de, double &depls,
+                                  double *s, double &syy)
+{
+    depls = 0;
+    double a1 = bulkm + 4. / 3 * shearm;
+    double a2 = bulkm - 2. / 3 * shearm;
+    double sxx = s[0] + de[1] * a2 + de[0] * a1;
+    double szz = s[1] + de[0] * a2 + de[1] * a1;
+    double sxz = s[2] + de[2] * 2 * shearm;
+    syy += (de[0] + de[1]) * a2;
+
+    double p[3];
+    double cos2t, sin2t;
+    int n1, n2, n3;
+    {
+        double s0 = 0.5 * (sxx + szz);
+        double rad = 0.5 * sqrt((sxx - szz) * (sxx - szz) + 4 * sxz * sxz);
+        double si = s0 - rad;
+        double sii = s0 + rad;
+        const double eps = 1e-15;
+        if (rad > eps) {
+            cos2t = 0.5 * (szz - sxx) / rad;
+            sin2t = -sxz / rad;
+        } else {
+            cos2t = 1;
+            sin2t = 0;
+        }
+        if (syy > sii) {
+            n1 = 0; n2 = 1; n3 = 2;
+            p[0] = si; p[1] = sii; p[2] = syy;
+        } else if (syy < si) {
+            n1 = 1; n2 = 2; n3 = 0;
+            p[0] = syy; p[1] = si; p[2] = sii;
+        } else {
+            n1 = 0; n2 = 2; n3 = 1;
+            p[0] = si; p[1] = syy; p[2] = sii;
+        }
+    }
+    if (p[0] >= ten_max) {
+        s[0] = s[1] = syy = ten_max;
+        s[2] = 0.0;
+        return;
+    }
+    if (p[1] >= ten_max) {
+        p[1] = p[2] = ten_max;
+    } else if (p[2] >= ten_max) {
+        p[2] = ten_max;
+    }
+    double fs = p[0] - p[2] * anphi + amc;
+    if (fs >= 0.0) {
+        s[0] = sxx;
+        s[1] = szz;
+        s[2] = sxz;
+        return;
+    }
+    const double alams = fs / (a1 - a2 * anpsi + a1 * anphi * anpsi - a2 * anphi + hardn);
+    p[0] -= alams * (a1 - a2 * anpsi);
+    p[1] -= alams * (a2 - a2 * anpsi);
+    p[2] -= alams * (a2 - a1 * anpsi);
+    depls = 0.5 * fabs(alams + alams * anpsi);
+    if (p[0] >= ten_max) {
+        s[0] = s[1] = syy = ten_max;
+        s[2] = 0.0;
+        return;
+    }
+    if (p[1] >= ten_max) {
+        p[1] = p[2] = ten_max;
+    } else if (p[2] >= ten_max) {
+        p[2] = ten_max;
+    }
+    double pn1 = (n1 == 0) ? p[0] : p[1];
+    double pn2 = (n2 == 1) ? p[1] : p[2];
+    double pn3 = (n3 == 0) ? p[0] : ((n3 == 1) ? p[1] : p[2]);
+    double dc2 = (pn1 - pn2) * cos2t;
+    double dss = pn1 + pn2;
+    s[0] = 0.5 * (dss + dc2);
+    s[1] = 0.5 * (dss - dc2);
+    s[2] = 0.5 * (pn1 - pn2) * sin2t;
+    syy = pn3;
+}
+
+// One element of update_stress (rheology.cxx:510-646).  In/out arrays are
+// the element's own values; dt = Variables::dt.  Returns a DES_DEV_* bit set.
+template <int ND>
+__device__ unsigned update_stress_elem(const KP &p, int e, double dt, double *s, double &syy, double *es,
+                                       double *edot, double &pls, double &dpls, double edvoldt, double vol,
+                                       double vol_old, double &dpressure)
+{
+    constexpr int NSTR = ND * (ND + 1) / 2;
+    unsigned bits = 0;
+    double old_s = trace_<ND>(s);
+    {
+        double div = trace_<ND>(edot);
+#pragma unroll
+        for (int i = 0; i < ND; ++i) edot[i] += (edvoldt - div) / ND;
+    }
+#pragma unroll
+    for (int i = 0; i < NSTR; ++i) es[i] += edot[i] * dt;
+    double de[NSTR];
+#pragma unroll
+    for (int i = 0; i < NSTR; ++i) de[i] = edot[i] * dt;
+
+    const int rt = p.mat.rheol_type;
+    if (rt == DES_RH_ELASTIC) {
+        elastic_<ND>(m_bulkm(p, e), m_shearm(p, e), de, s);
+    } else if (rt == DES_RH_VISCOUS) {
+        viscous_<ND>(m_bulkm(p, e), m_visc<ND>(p, e, edot), trace_<ND>(es), edot, s);
+    } else if (rt == DES_RH_MAXWELL) {
+        double dv = vol / vol_old - 1;
+        maxwell_<ND>(m_bulkm(p, e), m_shearm(p, e), m_visc<ND>(p, e, edot), dt, dv, de, s);
+    } else if (rt == DES_RH_EP) {
+        double depls = 0, amc, anphi, anpsi, hardn, ten_max;
+        double bulkm = m_bulkm(p, e), shearm = m_shearm(p, e);
+        m_plastic_props(p, e, pls, amc, anphi, anpsi, hardn, ten_max);
+        if (p.mat.is_plane_strain)
+            elasto_plastic2d_(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, s, syy);
+        else if (elasto_plastic_<ND>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, s))
+            bits |= DES_DEV_QL_NOCONV;
+        pls += depls;
+        dpls = depls;
+    } else if (rt == DES_RH_EVP) {
+        double depls = 0;
+        double bulkm = m_bulkm(p, e), shearm = m_shearm(p, e);
+        double viscosity = m_visc<ND>(p, e, edot);
+        double dv = vol / vol_old - 1;
+        double sv[NSTR];
+#pragma unroll
+        for (int i = 0; i < NSTR; ++i) sv[i] = s[i];
+        maxwell_<ND>(bulkm, shearm, viscosity, dt, dv, de, sv);
+        double svII = second_invariant2_<ND>(sv);
+        double amc, anphi, anpsi, hardn, ten_max;
+        m_plastic_props(p, e, pls, amc, anphi, anpsi, hardn, ten_max);
+        double sp[NSTR], spyy = syy;
+#pragma unroll
+        for (int i = 0; i < NSTR; ++i) sp[i] = s[i];
+        if (p.mat.is_plane_strain)
+            elasto_plastic2d_(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, sp, spyy);
+        else if (elasto_plastic_<ND>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, sp))
+            bits |= DES_DEV_QL_NOCONV;
+        double spII = second_invariant2_<ND>(sp);
+        if (svII < spII) {
+#pragma unroll
+            for (int i = 0; i < NSTR; ++i) s[i] = sv[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < NSTR; ++i) s[i] = sp[i];
+            pls += depls;
+            dpls = depls;
+            // rheology.cxx:632 copies spyy, which is initialised only in plane
+            // strain; elsewhere stressyy is left unchanged.
+            if (p.mat.is_plane_strain) syy = spyy;
+        }
+    }
+    dpressure = trace_<ND>(s) - old_s;
+    return bits;
+}
+
+}  // namespace des

@@ -1,0 +1,254 @@
+/*
+ * desgpu.h -- C ABI of the GB300-native explicit time-step library for
+ * DynEarthSol3D-style Lagrangian finite elements (linear triangles in 2D,
+ * linear tetrahedra in 3D).
+ *
+ * Every entry point returns an int status: DES_OK (0) on success, otherwise
+ * one of the DES_E* codes below.  DES_ERUNTIME (11) and DES_EASSERT (12)
+ * mirror the reference's std::exit codes ("11 runtime error", "12 assertion
+ * error", DEVELOPING:32-37), so a host shim can exit with the same code.
+ * The message of the last failure of a context is available through
+ * des_last_error().
+ *
+ * Data layout at the boundary follows the reference's host arrays
+ * (Array2D<T,N> rows, array2d.hpp:86-87: element i of a row-major [n][N]
+ * array starts at a + N*i).  Inside the library every field is kept on the
+ * device as structure-of-arrays.
+ *
+ * Threading: a context is used by one host thread at a time; all device work
+ * of a context runs in order on one CUDA stream, which the caller may supply.
+ */
+#ifndef DESGPU_H
+#define DESGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define DES_OK          0
+#define DES_EINPUT      1    /* invalid argument (reference code 1: user input error) */
+#define DES_ECUDA       3    /* a CUDA runtime call failed */
+#define DES_ENOMEM      4    /* device allocation failed */
+#define DES_ERUNTIME   11    /* numerical failure, e.g. dt <= 0 (geometry.cxx:304-308) */
+#define DES_EASSERT    12    /* internal consistency check failed */
+
+/* ---- sticky device error bits (des_device_status) --------------------- */
+#define DES_DEV_NONFINITE    1u  /* NaN/Inf met in a node coordinate or velocity */
+#define DES_DEV_NEG_VOLUME   2u  /* an element volume became <= 0 */
+#define DES_DEV_QL_NOCONV    4u  /* 3x3 QL eigen iteration hit its 30-sweep cap */
+#define DES_DEV_BAD_INDEX    8u  /* a connectivity or support index out of range */
+
+/* ---- constants shared with the reference ------------------------------ */
+#define DES_NBDRYTYPES 10           /* nbdrytypes, constants.hpp:38 */
+
+/* rheology bit set, MatProps::rh_* (matprops.hpp:47-53) */
+#define DES_RH_ELASTIC  1
+#define DES_RH_VISCOUS  2
+#define DES_RH_PLASTIC  4
+#define DES_RH_MAXWELL  (DES_RH_ELASTIC | DES_RH_VISCOUS)
+#define DES_RH_EP       (DES_RH_ELASTIC | DES_RH_PLASTIC)
+#define DES_RH_EVP      (DES_RH_ELASTIC | DES_RH_VISCOUS | DES_RH_PLASTIC)
+
+/* precision of a context */
+#define DES_PREC_FP64   0   /* every operation in FP64 */
+#define DES_PREC_MIXED  1   /* FP32 element kinematics/rheology increments, FP64 state and accumulation */
+
+/* ---- mesh ------------------------------------------------------------- */
+/* Topology of one mesh.  Mirrors Variables::{connectivity, bcflag, bfacets,
+ * bnormals, edge_vectors} (parameters.hpp:229-279).  The node-to-element
+ * support lists (Variables::support, mesh.cxx:1707-1721) are derived inside
+ * the library from the connectivity, in ascending element order. */
+typedef struct des_mesh {
+    int ndims;                    /* 2 or 3 */
+    int nnode;
+    int nelem;
+    const int *connectivity;      /* [nelem][ndims+1] node ids */
+    const unsigned *bcflag;       /* [nnode] BOUNDX0.. bit flags (constants.hpp:29-38) */
+    /* boundary facets: boundary i owns pairs [bfacet_offsets[i], bfacet_offsets[i+1]) */
+    const int *bfacet_offsets;    /* [DES_NBDRYTYPES+1] */
+    const int *bfacets;           /* [nbfacet][2] = (element, local facet 0..ndims) */
+    double bnormals[DES_NBDRYTYPES][3];                 /* unit outward normals */
+    double edge_vectors[DES_NBDRYTYPES][DES_NBDRYTYPES][3]; /* [i][j], i<j: boundary intersection edge */
+} des_mesh;
+
+/* ---- run-time parameters (the subset of Param the step reads) --------- */
+typedef struct des_params {
+    /* Control (parameters.hpp:81-101) */
+    double gravity;
+    double inertial_scaling;
+    double dt_fraction;
+    double fixed_dt;
+    double damping_factor;
+    double surface_diffusivity;
+    double max_vbc_val;           /* Variables::max_vbc_val (dynearthsol.cxx:36-39) */
+    int damping_option;
+    int ref_pressure_option;
+    int surface_process_option;   /* 0 only; other options stay on the host */
+    int is_quasi_static;
+    int has_thermal_diffusion;
+    /* BC (parameters.hpp:103-135) */
+    double surface_temperature;
+    double mantle_temperature;
+    double winkler_delta_rho;
+    double elastic_foundation_constant;
+    int has_fixed_bottom_temperature;
+    int has_winkler_foundation;
+    int has_elastic_foundation;
+    int has_water_loading;
+    int vbc_types[DES_NBDRYTYPES];     /* Variables::vbc_types, dynearthsol.cxx:43-52 */
+    double vbc_values[DES_NBDRYTYPES]; /* Variables::vbc_values, dynearthsol.cxx:54-63 */
+    /* Mesh */
+    double zlength;
+    /* compensation pressure of the Winkler foundation (Variables::compensation_pressure) */
+    double compensation_pressure;
+} des_params;
+
+/* ---- material table (Mat, parameters.hpp:166-194; MatProps) ---------- */
+/* Each array holds nmat entries.  scalar_mask bit k set means parameter k
+ * was given as a single value (VectorBase::create's Vector1, matprops.cxx:
+ * 176-187), for which the harmonic/arithmetic means return entry 0 unchanged
+ * (matprops.cxx:105,119).  Bits: 0 bulk_modulus, 1 shear_modulus,
+ * 2 heat_capacity, 3 radiogenic_heating, 4 therm_cond. */
+typedef struct des_material {
+    int rheol_type;          /* DES_RH_* */
+    int nmat;
+    int is_plane_strain;
+    unsigned scalar_mask;
+    double visc_min, visc_max, tension_max, therm_diff_max;
+    const double *rho0, *alpha;
+    const double *bulk_modulus, *shear_modulus;
+    const double *visc_exponent, *visc_coefficient, *visc_activation_energy;
+    const double *heat_capacity, *therm_cond, *radiogenic_heating;
+    const double *pls0, *pls1;
+    const double *cohesion0, *cohesion1;
+    const double *friction_angle0, *friction_angle1;
+    const double *dilation_angle0, *dilation_angle1;
+    const int *elemmarkers;  /* [nelem][nmat] marker counts, or NULL: one marker of material 0 */
+} des_material;
+
+/* ---- host state in the reference's layout (Variables fields) ---------- */
+/* Any pointer may be NULL in des_download_state (that field is skipped).
+ * In des_upload_state the fields marked (in) are required. */
+typedef struct des_host_state {
+    double *coord;          /* (in) [nnode][ndims] */
+    double *coord0;         /* [nnode][ndims]; NULL on upload = copy of coord */
+    double *vel;            /* (in) [nnode][ndims] */
+    double *force;          /* [nnode][ndims] */
+    double *temperature;    /* (in) [nnode] */
+    double *mass, *tmass, *volume_n, *ntmp;   /* [nnode] */
+    double *volume;         /* [nelem]; recomputed from coord on upload when NULL */
+    double *volume_old;     /* (in) [nelem] */
+    double *stress;         /* (in) [nelem][nstr] */
+    double *strain;         /* (in) [nelem][nstr] */
+    double *strain_rate;    /* [nelem][nstr] */
+    double *plstrain;       /* (in) [nelem] */
+    double *delta_plstrain; /* [nelem] */
+    double *stressyy;       /* [nelem] (plane strain) */
+    double *dpressure;      /* [nelem] */
+    double *edvoldt;        /* [nelem] */
+    double *shpdx, *shpdy, *shpdz;  /* [nelem][ndims+1]; shpdy unused in 2D */
+    double time;
+    double dt;
+    int steps;
+} des_host_state;
+
+typedef struct des_ctx des_ctx;
+
+/* Library version string. */
+const char *des_version(void);
+
+/* Create a context on the current CUDA device.  stream may be NULL (the
+ * library creates its own non-blocking stream).  precision is DES_PREC_*.
+ * Replaces the device half of allocate_variables (fields.cxx:10-48). */
+int des_create(const des_mesh *mesh, const des_params *param,
+               const des_material *mat, int precision, void *stream,
+               des_ctx **out);
+int des_destroy(des_ctx *ctx);
+
+/* Message of the last failure of ctx (or of the last failed des_create when
+ * ctx is NULL), copied into buf (always NUL-terminated). */
+int des_last_error(const des_ctx *ctx, char *buf, size_t len);
+
+/* Sticky device error bits (DES_DEV_*), read and cleared. */
+int des_device_status(des_ctx *ctx, unsigned *bits);
+
+/* Host <-> device state transfer (reference AoS layout <-> device SoA).
+ * des_upload_state replaces the host->device re-upload after init, restart
+ * and remesh (dynearthsol.cxx:80-99,179-215; remeshing.cxx:2009-2015);
+ * des_download_state is called before host readers (output.cxx:79-208). */
+int des_upload_state(des_ctx *ctx, const des_host_state *st);
+int des_download_state(des_ctx *ctx, des_host_state *st);
+
+/* Replace the parameters (e.g. after a change of max_vbc_val). */
+int des_set_params(des_ctx *ctx, const des_params *param);
+
+/* Per-element parameter overrides (extension used by the perturbed-cohesion
+ * and inverse-problem workloads; no counterpart in the reference, whose
+ * properties are per material).  field is DES_EF_*; values [nelem] on the
+ * host; NULL removes the override. */
+#define DES_EF_COHESION0      0   /* Pa, replaces the blended cohesion0 */
+#define DES_EF_COHESION1      1   /* Pa, replaces the blended cohesion1 */
+#define DES_EF_LOG10_VISC     2   /* log10(Pa s), replaces MatProps::visc before clamping */
+#define DES_EF_SHEAR_MODULUS  3   /* Pa, replaces MatProps::shearm */
+#define DES_EF_FRICTION0      4   /* degree, replaces friction_angle0 */
+#define DES_EF_FRICTION1      5   /* degree, replaces friction_angle1 */
+#define DES_EF_THERM_COND     6   /* W/m/K, replaces MatProps::k */
+#define DES_EF_COUNT          7
+int des_set_elem_field(des_ctx *ctx, int field, const double *values);
+
+/* ---- per-function entry points (device-resident state) --------------- */
+/* Each one replaces the reference function cited beside it, reading and
+ * writing the context's device copy of the corresponding Variables fields. */
+int des_update_temperature(des_ctx *ctx);  /* fields.cxx:96-163 (tdot -> ntmp) */
+int des_update_strain_rate(des_ctx *ctx);  /* fields.cxx:166-232 */
+int des_compute_dvoldt(des_ctx *ctx);      /* geometry.cxx:111-155 (-> ntmp) */
+int des_compute_edvoldt(des_ctx *ctx);     /* geometry.cxx:158-179 (ntmp -> edvoldt) */
+int des_update_stress(des_ctx *ctx);       /* rheology.cxx:510-646 */
+int des_NMD_stress(des_ctx *ctx);          /* geometry.cxx:182-236 (-> ntmp, stress) */
+int des_update_force(des_ctx *ctx);        /* fields.cxx:291-340 + bc.cxx:493-566 */
+int des_update_velocity(des_ctx *ctx);     /* fields.cxx:343-355 */
+int des_apply_vbcs(des_ctx *ctx);          /* bc.cxx:179-490 */
+int des_update_coordinate(des_ctx *ctx);   /* fields.cxx:358-368 */
+int des_swap_volume(des_ctx *ctx);         /* dynearthsol.cxx:226 volume <-> volume_old */
+int des_compute_volume(des_ctx *ctx);      /* geometry.cxx:86-108 */
+int des_compute_mass(des_ctx *ctx);        /* geometry.cxx:313-365 */
+int des_compute_shape_fn(des_ctx *ctx);    /* geometry.cxx:368-455 */
+int des_rotate_stress(des_ctx *ctx);       /* fields.cxx:411-483 */
+int des_compute_dt(des_ctx *ctx, double *dt_out); /* geometry.cxx:239-310; also sets the context dt */
+int des_update_mesh(des_ctx *ctx);         /* dynearthsol.cxx:221-232 (surface_process_option 0) */
+
+/* Worst element quality and its index (geometry.cxx:458-512, used by
+ * bad_mesh_quality, remeshing.cxx:1882-1935). */
+int des_worst_elem_quality(des_ctx *ctx, double *quality, int *elem);
+
+/* Read or set the context's dt / time / steps (Variables::dt, time, steps). */
+int des_get_clock(des_ctx *ctx, double *time, double *dt, int *steps);
+int des_set_clock(des_ctx *ctx, double time, double dt, int steps);
+
+/* ---- whole steps ------------------------------------------------------ */
+/* Run nsteps explicit steps: the body of the reference's time loop
+ * (dynearthsol.cxx:325-361) without phase changes, output and remeshing,
+ * with compute_dt every 10th step on the device.  Uses the fused kernel
+ * schedule; results equal the per-function sequence. */
+int des_step(des_ctx *ctx, int nsteps);
+
+/* Same as des_step, but with the state in HOST memory in the reference's
+ * layout: uploads st, runs nsteps, downloads into st (all inside the call).
+ * This is the drop-in form for a caller whose Variables stay authoritative. */
+int des_step_host(des_ctx *ctx, des_host_state *st, int nsteps);
+
+/* Synchronise the context's stream. */
+int des_synchronize(des_ctx *ctx);
+
+/* Number of CUDA kernel launches made by the context so far. */
+int des_launch_count(des_ctx *ctx, long long *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DESGPU_H */

@@ -1,0 +1,91 @@
+"""Generate the golden fixtures of tests/golden/ from the REFERENCE itself.
+
+Runs only where the reference tree exists (it compiles the reference's own
+fields/geometry/rheology/matprops/bc/ic sources and 3x3-C through
+``make -C oracle ref`` and drives them with oracle/ref_harness.cxx).  For
+every case of tests/cases.py it stores, bit for bit:
+
+* ``init/*``  -- the state after the reference's init sequence
+  (dynearthsol.cxx:82-98: volumes, masses, shape functions, boundary
+  normals, velocity BCs, initial stress, weak zone, dt);
+* ``final/*`` -- the state after ``nsteps`` of the loop body
+  (dynearthsol.cxx:325-361) and the dt of every step;
+* for the per-function cases, ``mid/*`` (the state after 60 steps) and
+  ``fn_<name>/*`` -- the fields each reference function writes when applied
+  once to ``mid`` (plus compute_dt and worst_elem_quality results).
+
+Usage:  python tests/golden/gen_golden.py [case ...]
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from dataclasses import replace  # noqa: E402
+
+from cases import CASES, FUNCTIONS, PERFN_CASES, PERFN_MID_STEPS, build_case, reference_material_for  # noqa: E402
+from dynearthsol_gb300.config import initial_state  # noqa: E402
+from oracle.oracle import Reference, build_reference, state_copy  # noqa: E402
+
+
+def gen(name: str) -> str:
+    wl, nsteps = build_case(name)
+    wl_ref = replace(wl, mat=reference_material_for(wl), elem_fields={})
+    ref = Reference(wl.mesh.ndims)
+    st, comp = initial_state(wl)
+    out = {}
+    bn, ev, cp, clk = ref.init(wl_ref, st)
+    for k, v in st.items():
+        out[f"init/{k}"] = v.copy()
+    out["init/bnormals"] = bn
+    out["init/edge_vectors"] = ev
+    out["init/clock"] = np.array(clk, dtype=np.float64)
+    out["init/compensation_pressure"] = np.array(cp)
+    if name in PERFN_CASES:
+        mid = state_copy(st)
+        clk_mid, _ = ref.run(wl_ref, mid, cp, clk, PERFN_MID_STEPS)
+        for k, v in mid.items():
+            out[f"mid/{k}"] = v.copy()
+        out["mid/clock"] = np.array(clk_mid, dtype=np.float64)
+        for fn, fields in FUNCTIONS.items():
+            s = state_copy(mid)
+            ref.call(wl_ref, s, cp, clk_mid, fn)
+            for f in fields:
+                out[f"fn_{fn}/{f}"] = s[f].copy()
+        s = state_copy(mid)
+        res, _ = ref.call(wl_ref, s, cp, clk_mid, "compute_dt")
+        out["fn_compute_dt/dt"] = np.array(res[0])
+        s = state_copy(mid)
+        res, _ = ref.call(wl_ref, s, cp, clk_mid, "worst_elem_quality")
+        out["fn_worst_elem_quality/result"] = res.copy()
+    clk_f, dts = ref.run(wl_ref, st, cp, clk, nsteps)
+    for k, v in st.items():
+        out[f"final/{k}"] = v.copy()
+    out["final/clock"] = np.array(clk_f, dtype=np.float64)
+    out["final/dts"] = dts
+    out["nsteps"] = np.array(nsteps)
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
+def main(argv):
+    if not build_reference():
+        print("reference tree not found; cannot generate fixtures", file=sys.stderr)
+        return 1
+    names = argv or CASES
+    for n in names:
+        p = gen(n)
+        print(f"{n}: {os.path.getsize(p) / 1024:.1f} KiB")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))
