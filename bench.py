@@ -1,0 +1,354 @@
+"""Benchmark of the explicit time step on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+                    [--workload c1_3d_evp] [--impl reference]
+
+A "step" is one explicit time step (the body of the reference's time loop,
+dynearthsol.cxx:325-361) over the whole mesh.  The default workload is the
+3D 100x100x10 km box of 80x80x26 cubes x 6 = 998,400 tetrahedra (177,147
+nodes), Maxwell visco-elasto-plastic with Arrhenius viscosity and
+Mohr-Coulomb plasticity, thermal diffusion on.  Its device state (~310 MB)
+is larger than the 129 MB L2, so consecutive steps stream from HBM.
+
+Metric: Mtet-steps/s = nelem x steps / time (higher is better).
+* value:   device-resident state, the CUDA-graph step replayed K times, timed
+           with CUDA events on the library's stream, max over ranks;
+* e2e:     the drop-in call des_step_host with the state in pinned host
+           memory in the reference's layout, uploaded and downloaded every
+           step (host<->device copies inside the timed region);
+* roofline: the dominant kernel (update_stress) timed alone with CUDA
+           events: algorithmic bytes per launch / duration against the
+           measured HBM copy bandwidth (MEASURED_PEAKS.json);
+* cpu_baseline: the oracle (C restatement of the reference, OpenMP with the
+           reference's two-colour band scatter) on this host's cores, on a
+           bounded sample of the same workload.
+--impl reference times that CPU implementation alone on the same workload.
+With --gpus N > 1 (torchrun) every rank runs an independent replica
+(the path has no data-path exchange on one GPU per replica): "weak" scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# bytes per element of update_stress that must cross HBM once per launch:
+# reads stress, strain, strain_rate (3 x 48), plstrain, delta_plstrain,
+# stressyy, edvoldt, volume, volume_old (6 x 8), connectivity (16);
+# writes stress, strain, strain_rate (3 x 48), plstrain, delta_plstrain,
+# stressyy, dpressure (4 x 8); node temperatures are counted per node.
+STRESS_BYTES_PER_ELEM_FP64 = 3 * 48 + 6 * 8 + 16 + 3 * 48 + 4 * 8
+# compulsory bytes of a whole step per tet (3D FP64): element state read and
+# written once, support lists read once, node state read and written once
+STEP_ELEM_BYTES = 16 + 96 + 96 + 16 + 16          # conn, stress r/w, strain r/w, plstrain r/w, volume old/new
+SUPPORT_BYTES_PER_ELEM = 16
+NODE_BYTES = 48 + 48 + 16 + 4                       # coord r/w, vel r/w, T r/w, bcflag
+
+
+def step_bytes_per_tet(nn, ne):
+    return STEP_ELEM_BYTES + SUPPORT_BYTES_PER_ELEM + (NODE_BYTES + 4) * nn / ne
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str, workload: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(wl, st, cp, clock, nthreads, budget_s=12.0):
+    """Oracle (CPU restatement, OpenMP) on the same workload: a bounded
+    number of steps sized to ~budget_s seconds."""
+    from oracle.oracle import Oracle, state_copy
+    s = state_copy(st)
+    o = Oracle(wl, s, cp, nthreads, clock)
+    t0 = time.perf_counter()
+    o.run(2)
+    t_cal = (time.perf_counter() - t0) / 2
+    nsteps = int(max(2, min(200, budget_s / max(t_cal, 1e-6))))
+    t0 = time.perf_counter()
+    rc = o.run(nsteps)
+    dt = time.perf_counter() - t0
+    if rc:
+        raise RuntimeError(f"oracle run failed ({rc})")
+    return {"value": wl.mesh.nelem * nsteps / dt / 1e6, "unit": "Mtet-steps/s", "cores": nthreads,
+            "kind": "port",
+            "sample": f"{nsteps} steps of the full {wl.mesh.nelem:,}-tet workload, "
+                      f"OpenMP x{nthreads} (two-colour element bands), {dt:.1f} s"}
+
+
+def setup_workload(name):
+    from dynearthsol_gb300.config import initial_state, make_workload
+    wl = make_workload(name)
+    st, cp = initial_state(wl)
+    return wl, st, cp
+
+
+def run_reference(args, rank, world):
+    """CPU implementation (oracle port) on this host, all threads."""
+    if rank != 0:
+        return 0
+    wl, st, cp = setup_workload(args.workload)
+    from oracle.oracle import Oracle
+    nthreads = os.cpu_count() or 1
+    o = Oracle(wl, st, cp, nthreads)
+    o.init_fields()
+    clock = o.clock
+    for _ in range(args.warmup):
+        o.run(1)
+    # each timed step is one explicit step of the full workload
+    t0 = time.perf_counter()
+    rc = o.run(args.steps)
+    el = time.perf_counter() - t0
+    if rc:
+        raise RuntimeError(f"oracle failed ({rc})")
+    v = wl.mesh.nelem * args.steps / el / 1e6
+    line = {
+        "impl": "reference", "metric": metric_name(args), "value": v, "unit": "Mtet-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_of(args, wl),
+        "cpu_baseline": {"value": v, "unit": "Mtet-steps/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{args.steps} timed steps (after {args.warmup} warm-up) of the full "
+                                   f"{wl.mesh.nelem:,}-tet workload, OpenMP x{nthreads}"},
+        "e2e": {"value": v, "unit": "Mtet-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def metric_name(args):
+    return "Mtet-steps/s"
+
+
+def config_of(args, wl):
+    return {"workload": args.workload, "nelem": wl.mesh.nelem, "nnode": wl.mesh.nnode,
+            "precision": args.precision, "physics": wl.description,
+            "l2_policy": "inputs larger than L2 (device state > 129 MB), no flush",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default="c1_3d_evp")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.solver import DeviceModel
+
+    wl, st0, cp = setup_workload(args.workload)
+    prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
+    stream = torch.cuda.Stream()
+    m = DeviceModel(wl, comp_pressure=cp, precision=prec, stream=stream.cuda_stream)
+    init = m.init_fields(st0)
+    clock0 = m.clock()
+
+    # ---- device-resident throughput ----
+    m.step(args.warmup)
+    m.sync()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    l0 = m.launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    m.step(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = m.launches() - l0
+    clocks = sampler.stop()
+    status = m.device_status()
+    if status:
+        raise RuntimeError(f"device status {status:#x} during the timed run")
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    ne, nn = wl.mesh.nelem, wl.mesh.nnode
+    value = world * ne * args.steps / (ms_max / 1e3) / 1e6
+
+    # ---- dominant kernel alone (update_stress) for the roofline ----
+    m.upload(init, clock0)
+    m.step(2)
+    ks0, ks1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    m.call("update_stress")
+    torch.cuda.synchronize()
+    ks0.record(stream)
+    for _ in range(reps):
+        m.call("update_stress")
+    ks1.record(stream)
+    torch.cuda.synchronize()
+    k_ms = ks0.elapsed_time(ks1) / reps
+    hbm_peak, peak_kind = measured_peaks()
+    alg = STRESS_BYTES_PER_ELEM_FP64 * ne + 16 * nn
+    achieved = alg / (k_ms / 1e3) / 1e9
+    traffic = profile_traffic("update_stress", args.workload)
+    roofline = {"bound": "hbm", "kernel": "k_update_stress", "achieved": achieved, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                "kernel_ms": k_ms, "algorithmic_bytes_per_launch": alg,
+                "peak_kind": peak_kind,
+                "note": "FP64 update_stress is bound by the FP64 pipe (GB300 FP64 ~1/64 of FP32), not HBM"}
+    step_alg = step_bytes_per_tet(nn, ne)
+    step_gbs = step_alg * ne * args.steps / (ms_max / 1e3) / 1e9
+
+    # ---- end to end through the host-buffer drop-in call ----
+    from dynearthsol_gb300 import capi as _c
+    pinned = {}
+    for k, v in init.items():
+        tt = torch.empty(v.shape, dtype=torch.float64, pin_memory=True)
+        a = tt.numpy()
+        a[...] = v
+        pinned[k] = (tt, a)
+    hs = {k: a for k, (tt, a) in pinned.items()}
+    h2d = sum(a.nbytes for k, a in hs.items()
+              if k not in ("shpdy",) or wl.mesh.ndims == 3)
+    d2h = h2d
+    clk = clock0
+    for _ in range(2):
+        clk = m.step_host(hs, 1, clk)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        clk = m.step_host(hs, 1, clk)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * ne * args.e2e_steps / float(te.item()) / 1e6
+
+    if rank == 0:
+        line = {
+            "metric": metric_name(args), "value": value, "unit": "Mtet-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (structured box mesh, seeded; no dataset)",
+            "config": config_of(args, wl),
+            "roofline": roofline,
+            "step_hbm": {"algorithmic_bytes_per_tet": step_alg, "achieved_gbs": step_gbs,
+                         "frac": step_gbs / hbm_peak},
+            "e2e": {"value": e2e_value, "unit": "Mtet-steps/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+                    "call": "des_step_host (pinned host state, reference AoS layout, 1 step per call)"},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(wl, init, cp, clock0, os.cpu_count() or 1)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    m.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -21,6 +21,32 @@
 #include <omp.h>
 #endif
 
+#ifdef DES_ORACLE_PERTURB_LIBM
+/* Sensitivity probe (a separate build, liboracle_pert.so): every libm
+ * transcendental result is moved by -1, 0 or +1 ulp, pseudo-randomly, to
+ * measure how far the reference's own algorithm drifts when its libm
+ * differs in the last bit -- the envelope inside which any other faithful
+ * implementation (another libm, another processor) must land. */
+static unsigned long long pert_state = 88172645463325252ull;
+void oracle_perturb_seed(unsigned long long s) { pert_state = s ? s : 88172645463325252ull; }
+static double pert_(double x)
+{
+    pert_state ^= pert_state << 13;
+    pert_state ^= pert_state >> 7;
+    pert_state ^= pert_state << 17;
+    int r = (int)(pert_state % 3);
+    if (r == 0) return nextafter(x, INFINITY);
+    if (r == 1) return nextafter(x, -INFINITY);
+    return x;
+}
+#define sin(x) pert_(sin(x))
+#define cos(x) pert_(cos(x))
+#define tan(x) pert_(tan(x))
+#define pow(a, b) pert_(pow(a, b))
+#define exp(x) pert_(exp(x))
+#define atan2(a, b) pert_(atan2(a, b))
+#endif
+
 #define MAXND 3
 #define MAXNPE 4
 #define MAXNSTR 6

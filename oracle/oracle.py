@@ -21,14 +21,16 @@ from dynearthsol_gb300.config import CStructs, Workload, nstr_of
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBORACLE = os.path.join(HERE, "liboracle.so")
+LIBORACLE_PERT = os.path.join(HERE, "liboracle_pert.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 
-def build_oracle(force: bool = False) -> str:
+def build_oracle(force: bool = False, perturbed: bool = False) -> str:
     src = os.path.join(HERE, "des_oracle.c")
-    if force or not os.path.exists(LIBORACLE) or os.path.getmtime(LIBORACLE) < os.path.getmtime(src):
+    lib = LIBORACLE_PERT if perturbed else LIBORACLE
+    if force or not os.path.exists(lib) or os.path.getmtime(lib) < os.path.getmtime(src):
         subprocess.check_call(["make", "-s", "-C", HERE, "all"])
-    return LIBORACLE
+    return lib
 
 
 def build_reference() -> bool:
@@ -66,8 +68,13 @@ class Oracle:
     """The C restatement bound to one workload and one state dict."""
 
     def __init__(self, wl: Workload, st: dict, comp_pressure: float, nthreads: int = 1,
-                 clock=(0.0, 0.0, 0)):
-        self.lib = C.CDLL(build_oracle())
+                 clock=(0.0, 0.0, 0), perturb_seed: int | None = None):
+        """perturb_seed selects the libm-sensitivity build (transcendental
+        results moved by +-1 ulp, seeded)."""
+        self.lib = C.CDLL(build_oracle(perturbed=perturb_seed is not None))
+        if perturb_seed is not None:
+            self.lib.oracle_perturb_seed.argtypes = [C.c_ulonglong]
+            self.lib.oracle_perturb_seed(perturb_seed)
         L = self.lib
         L.oracle_create.restype = C.c_void_p
         L.oracle_create.argtypes = [C.POINTER(capi.DesMesh), C.POINTER(capi.DesParams),

@@ -10,9 +10,15 @@ every case of tests/cases.py it stores, bit for bit:
   normals, velocity BCs, initial stress, weak zone, dt);
 * ``final/*`` -- the state after ``nsteps`` of the loop body
   (dynearthsol.cxx:325-361) and the dt of every step;
-* for the per-function cases, ``mid/*`` (the state after 60 steps) and
+* for the per-function cases, ``mid/*`` (the state after 60 steps),
   ``fn_<name>/*`` -- the fields each reference function writes when applied
-  once to ``mid`` (plus compute_dt and worst_elem_quality results).
+  once to ``mid`` (plus compute_dt and worst_elem_quality results) -- and
+  ``mid1/*``, ``mid10/*``: the state 1 and 10 steps after ``mid``;
+* ``envelope/<field>`` -- the libm sensitivity of the case: the largest
+  normalised deviation from ``final`` of three runs of the restatement whose
+  transcendental results are moved by +-1 ulp (seeds 1, 2, 3).  Any faithful
+  FP64 implementation with a different libm lands inside a small multiple of
+  it; plastic 3D cases are chaotic enough that it exceeds 1e-9.
 
 Usage:  python tests/golden/gen_golden.py [case ...]
 """
@@ -32,7 +38,9 @@ from dataclasses import replace  # noqa: E402
 
 from cases import CASES, FUNCTIONS, PERFN_CASES, PERFN_MID_STEPS, build_case, reference_material_for  # noqa: E402
 from dynearthsol_gb300.config import initial_state  # noqa: E402
-from oracle.oracle import Reference, build_reference, state_copy  # noqa: E402
+from oracle.oracle import Oracle, Reference, build_reference, state_copy  # noqa: E402
+
+ENVELOPE_FIELDS = ("vel", "stress", "temperature", "plstrain", "coord", "strain")
 
 
 def gen(name: str) -> str:
@@ -59,15 +67,34 @@ def gen(name: str) -> str:
             ref.call(wl_ref, s, cp, clk_mid, fn)
             for f in fields:
                 out[f"fn_{fn}/{f}"] = s[f].copy()
+        for k_steps in (1, 10):
+            s = state_copy(mid)
+            clk_k, _ = ref.run(wl_ref, s, cp, clk_mid, k_steps)
+            for k, v in s.items():
+                out[f"mid{k_steps}/{k}"] = v.copy()
+            out[f"mid{k_steps}/clock"] = np.array(clk_k, dtype=np.float64)
         s = state_copy(mid)
         res, _ = ref.call(wl_ref, s, cp, clk_mid, "compute_dt")
         out["fn_compute_dt/dt"] = np.array(res[0])
         s = state_copy(mid)
         res, _ = ref.call(wl_ref, s, cp, clk_mid, "worst_elem_quality")
         out["fn_worst_elem_quality/result"] = res.copy()
+    init_state = state_copy(st)
     clk_f, dts = ref.run(wl_ref, st, cp, clk, nsteps)
     for k, v in st.items():
         out[f"final/{k}"] = v.copy()
+    env = {f: 0.0 for f in ENVELOPE_FIELDS}
+    for seed in (1, 2, 3):
+        s = state_copy(init_state)
+        o = Oracle(wl, s, cp, 1, (clk[0], clk[1], int(clk[2])), perturb_seed=seed)
+        assert o.run(nsteps) == 0
+        for f in ENVELOPE_FIELDS:
+            scale = np.abs(st[f]).max()
+            d = np.abs(s[f] - st[f]).max()
+            env[f] = max(env[f], float(d / scale) if scale else float(d))
+        del o
+    for f, v in env.items():
+        out[f"envelope/{f}"] = np.array(v)
     out["final/clock"] = np.array(clk_f, dtype=np.float64)
     out["final/dts"] = dts
     out["nsteps"] = np.array(nsteps)

@@ -98,6 +98,29 @@ def test_oracle_dt_and_quality_match_reference(name):
     assert abs(q - ref[0]) <= max(TOL, 0) * abs(q) + (0 if EXACT else 1e-15)
 
 
+@pytest.mark.parametrize("name", PERFN_CASES)
+def test_oracle_steps_from_mid_match_reference(name):
+    g = load_golden(name)
+    wl, _ = build_case(name)
+    for k_steps in (1, 10):
+        st = state_from(g["mid"])
+        clk = tuple(g["mid"]["clock"])
+        o = Oracle(wl, st, float(g["init"]["compensation_pressure"]), clock=(clk[0], clk[1], int(clk[2])))
+        assert o.run(k_steps) == 0
+        compare(st, g[f"mid{k_steps}"], fields=[k for k in g[f"mid{k_steps}"] if k != "clock"],
+                label=f"mid+{k_steps} ")
+
+
+def test_libm_envelope_recorded():
+    """Every fixture records its libm-sensitivity envelope; plastic 3D runs
+    are the chaotic ones."""
+    for name in CASES:
+        g = load_golden(name)
+        assert set(g["envelope"]) >= {"vel", "stress", "temperature", "plstrain"}
+    assert float(load_golden("3d_evp_yield")["envelope"]["stress"]) > 1e-9
+    assert float(load_golden("2d_ep")["envelope"]["stress"]) < 1e-12
+
+
 def test_plasticity_is_exercised():
     """The yield cases really go through the Mohr-Coulomb return map."""
     for name in ("2d_ep_yield", "3d_evp_yield", "3d_ep_yield", "3d_heat_jitter_multimat", "2d_ps_oedometer"):
