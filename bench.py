@@ -296,7 +296,37 @@ def main():
     step_gbs = step_alg * ne * args.steps / (ms_max / 1e3) / 1e9
 
     # ---- end to end through the host-buffer drop-in call ----
-    from dynearthsol_gb300 import capi as _c
+    e2e = None
+    if args.e2e_steps > 0:
+        e2e = run_e2e(args, m, wl, init, clock0, world, dist)
+    if rank == 0:
+        line = {
+            "metric": metric_name(args), "value": value, "unit": "Mtet-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (structured box mesh, seeded; no dataset)",
+            "config": config_of(args, wl),
+            "roofline": roofline,
+            "step_hbm": {"algorithmic_bytes_per_tet": step_alg, "achieved_gbs": step_gbs,
+                         "frac": step_gbs / hbm_peak},
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(wl, init, cp, clock0, os.cpu_count() or 1)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    m.close()
+    return 0
+
+
+def run_e2e(args, m, wl, init, clock0, world, dist):
+    import torch
+    ne = wl.mesh.nelem
     pinned = {}
     for k, v in init.items():
         tt = torch.empty(v.shape, dtype=torch.float64, pin_memory=True)
@@ -313,6 +343,7 @@ def main():
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
+    hs = {k: a for k, (tt, a) in pinned.items()}
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         clk = m.step_host(hs, 1, clk)
@@ -322,32 +353,9 @@ def main():
     if dist:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
     e2e_value = world * ne * args.e2e_steps / float(te.item()) / 1e6
-
-    if rank == 0:
-        line = {
-            "metric": metric_name(args), "value": value, "unit": "Mtet-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-            "data": "synthetic (structured box mesh, seeded; no dataset)",
-            "config": config_of(args, wl),
-            "roofline": roofline,
-            "step_hbm": {"algorithmic_bytes_per_tet": step_alg, "achieved_gbs": step_gbs,
-                         "frac": step_gbs / hbm_peak},
-            "e2e": {"value": e2e_value, "unit": "Mtet-steps/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
-                    "call": "des_step_host (pinned host state, reference AoS layout, 1 step per call)"},
-            "gpu_launches": int(launches),
-            "clocks": clocks,
-        }
-        if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(wl, init, cp, clock0, os.cpu_count() or 1)
-        print(json.dumps(line), flush=True)
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
-    m.close()
-    return 0
+    return {"value": e2e_value, "unit": "Mtet-steps/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+            "call": "des_step_host (pinned host state, reference AoS layout, 1 step per call)"}
 
 
 if __name__ == "__main__":

@@ -13,7 +13,8 @@ every case of tests/cases.py it stores, bit for bit:
 * for the per-function cases, ``mid/*`` (the state after 60 steps),
   ``fn_<name>/*`` -- the fields each reference function writes when applied
   once to ``mid`` (plus compute_dt and worst_elem_quality results) -- and
-  ``mid1/*``, ``mid10/*``: the state 1 and 10 steps after ``mid``;
+  ``mid1/*``, ``mid10/*``: the state 1 and 10 steps after ``mid``, with
+  their envelopes ``envelope_mid1/*``, ``envelope_mid10/*`` (below);
 * ``envelope/<field>`` -- the libm sensitivity of the case: the largest
   normalised deviation from ``final`` of three runs of the restatement whose
   transcendental results are moved by +-1 ulp (seeds 1, 2, 3).  Any faithful
@@ -41,6 +42,22 @@ from dynearthsol_gb300.config import initial_state  # noqa: E402
 from oracle.oracle import Oracle, Reference, build_reference, state_copy  # noqa: E402
 
 ENVELOPE_FIELDS = ("vel", "stress", "temperature", "plstrain", "coord", "strain")
+
+
+def envelope(wl, start, cp, clk, nsteps, result):
+    """Largest normalised deviation from ``result`` over three runs of the
+    restatement with +-1 ulp perturbed transcendentals (seeds 1, 2, 3)."""
+    env = {f: 0.0 for f in ENVELOPE_FIELDS}
+    for seed in (1, 2, 3):
+        s = state_copy(start)
+        o = Oracle(wl, s, cp, 1, (clk[0], clk[1], int(clk[2])), perturb_seed=seed)
+        assert o.run(nsteps) == 0
+        for f in ENVELOPE_FIELDS:
+            scale = np.abs(result[f]).max()
+            d = np.abs(s[f] - result[f]).max()
+            env[f] = max(env[f], float(d / scale) if scale else float(d))
+        del o
+    return env
 
 
 def gen(name: str) -> str:
@@ -73,6 +90,8 @@ def gen(name: str) -> str:
             for k, v in s.items():
                 out[f"mid{k_steps}/{k}"] = v.copy()
             out[f"mid{k_steps}/clock"] = np.array(clk_k, dtype=np.float64)
+            for f, v in envelope(wl, mid, cp, clk_mid, k_steps, s).items():
+                out[f"envelope_mid{k_steps}/{f}"] = np.array(v)
         s = state_copy(mid)
         res, _ = ref.call(wl_ref, s, cp, clk_mid, "compute_dt")
         out["fn_compute_dt/dt"] = np.array(res[0])
@@ -83,17 +102,7 @@ def gen(name: str) -> str:
     clk_f, dts = ref.run(wl_ref, st, cp, clk, nsteps)
     for k, v in st.items():
         out[f"final/{k}"] = v.copy()
-    env = {f: 0.0 for f in ENVELOPE_FIELDS}
-    for seed in (1, 2, 3):
-        s = state_copy(init_state)
-        o = Oracle(wl, s, cp, 1, (clk[0], clk[1], int(clk[2])), perturb_seed=seed)
-        assert o.run(nsteps) == 0
-        for f in ENVELOPE_FIELDS:
-            scale = np.abs(st[f]).max()
-            d = np.abs(s[f] - st[f]).max()
-            env[f] = max(env[f], float(d / scale) if scale else float(d))
-        del o
-    for f, v in env.items():
+    for f, v in envelope(wl, init_state, cp, clk, nsteps, st).items():
         out[f"envelope/{f}"] = np.array(v)
     out["final/clock"] = np.array(clk_f, dtype=np.float64)
     out["final/dts"] = dts

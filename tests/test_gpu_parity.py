@@ -91,8 +91,8 @@ def test_gpu_step_matches_reference(name):
 @pytest.mark.parametrize("name", PERFN_CASES)
 @pytest.mark.parametrize("k_steps,tol", [(1, 1e-12), (10, 1e-10)])
 def test_gpu_steps_from_mid_state(name, k_steps, tol):
-    """Short runs from a mid-run reference state (plasticity active): the
-    device step agrees with the reference before chaotic growth sets in."""
+    """Short runs from a mid-run reference state (plasticity active): one
+    step agrees to 1e-12; ten steps to 1e-10 or the ten-step envelope."""
     g = load_golden(name)
     wl, _ = build_case(name)
     m = _model(wl, float(g["init"]["compensation_pressure"]))
@@ -101,8 +101,9 @@ def test_gpu_steps_from_mid_state(name, k_steps, tol):
     m.step(k_steps)
     out = m.download()
     ref = g[f"mid{k_steps}"]
+    env = max(float(v) for v in g[f"envelope_mid{k_steps}"].values())
     fields = [k for k in ref if k in out and k != "clock" and not (wl.mesh.ndims == 2 and k == "shpdy")]
-    _cmp(out, ref, fields, tol, f"mid+{k_steps}")
+    _cmp(out, ref, fields, max(tol, ENV_MARGIN * env), f"mid+{k_steps}")
 
 
 @pytest.mark.parametrize("name", PERFN_CASES)
@@ -191,23 +192,60 @@ def test_gpu_deterministic_and_step_host():
     assert clk2 == m1.clock()
 
 
-def test_gpu_longer_run_vs_oracle():
-    """The 3D visco-elasto-plastic workload at a reduced mesh (12x12x4 cubes,
-    3,456 tets) for 1000 steps: FP64 device vs the oracle's serial run."""
-    from dynearthsol_gb300.config import initial_state, make_workload
+def _long_run(wl, nsteps, perturb_seeds=()):
+    """Device and oracle runs of nsteps from the same initial state; returns
+    the normalised device errors and the perturbed-oracle envelope."""
+    from dynearthsol_gb300.config import initial_state
     from oracle.oracle import Oracle, state_copy
-    wl = make_workload("c1_3d_evp", cells=(12, 12, 4))
     st, cp = initial_state(wl)
     o = Oracle(wl, st, cp)
     assert o.init_fields() == 0
+    st0, clk0 = state_copy(st), o.clock
     m = _model(wl, cp)
-    m.upload(state_copy(st), o.clock)
-    m.step(1000)
-    assert o.run(1000) == 0
+    m.upload(state_copy(st0), clk0)
+    m.step(nsteps)
+    assert o.run(nsteps) == 0
     out = m.download()
-    errs = _cmp(out, st, KEY_FIELDS, 1e-9, "1000 steps")
     assert m.clock()[2] == o.clock[2]
+    errs = {k: rel_err(out[k], st[k]) for k in KEY_FIELDS}
+    env = {k: 0.0 for k in KEY_FIELDS}
+    for seed in perturb_seeds:
+        sp = state_copy(st0)
+        op = Oracle(wl, sp, cp, 1, clk0, perturb_seed=seed)
+        assert op.run(nsteps) == 0
+        for k in KEY_FIELDS:
+            env[k] = max(env[k], rel_err(sp[k], st[k]))
+    return errs, env
+
+
+def test_gpu_1000_steps_elastic_bit_exact_vs_oracle():
+    """Elastic rheology with heat diffusion on the 3D workload's mesh family
+    (12x12x4 cubes, 3,456 tets), 1000 steps.  This path calls no
+    transcendental function, so the FP64 device (no FMA contraction,
+    reference expression order, IEEE division and square root) must
+    reproduce the oracle -- and with it the reference -- bit for bit."""
+    from dataclasses import replace
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import make_workload
+    wl = make_workload("c1_3d_evp", cells=(12, 12, 4))
+    wl.mat = replace(wl.mat, rheol_type=capi.RH_ELASTIC)
+    errs, _ = _long_run(wl, 1000)
     print("normalised errors after 1000 steps:", errs)
+    assert max(errs.values()) == 0.0, errs
+
+
+def test_gpu_1000_steps_evp_within_libm_envelope():
+    """The 3D visco-elasto-plastic workload physics at 12x12x4 cubes, 1000
+    steps.  The reference's step is chaotic here (its min-J2 choice between
+    the Maxwell and elasto-plastic candidates and its copysign damping are
+    discontinuous), so the device is held to 20x the drift the oracle itself
+    shows when its libm results move by one ulp (two seeds, same run)."""
+    from dynearthsol_gb300.config import make_workload
+    wl = make_workload("c1_3d_evp", cells=(12, 12, 4))
+    errs, env = _long_run(wl, 1000, perturb_seeds=(1, 2))
+    print("normalised errors:", errs, "envelope:", env)
+    for k in KEY_FIELDS:
+        assert errs[k] <= max(1e-9, ENV_MARGIN * env[k]), (k, errs[k], env[k])
 
 
 def test_gpu_error_status_nan_and_negative_volume():
