@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -12,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "des_kernels.cuh"
+#include "des_mixed.cuh"
 
 using namespace des;
 
@@ -92,6 +94,8 @@ void invalidate_graph(des_ctx *c)
     }
 }
 
+void set_rho_pseudo(des_ctx *c);
+
 int set_params(des_ctx *c, const des_params *prm)
 {
     if (prm->ref_pressure_option != 0)
@@ -104,6 +108,7 @@ int set_params(des_ctx *c, const des_params *prm)
     if (prm->damping_option < 0 || prm->damping_option > 4)
         return fail_msg(c->err, DES_EINPUT, "unknown damping_option: %d", prm->damping_option);
     c->kp.prm = *prm;
+    set_rho_pseudo(c);
     invalidate_graph(c);
     return DES_OK;
 }
@@ -137,7 +142,23 @@ int set_material(des_ctx *c, const des_material *m)
         if (!src[k]) return fail_msg(c->err, DES_EINPUT, "material array %d is NULL", k);
         for (int i = 0; i < m->nmat; ++i) dst[k][i] = src[k][i];
     }
+    for (int i = 0; i < m->nmat; ++i) {
+        t.visc_pw[i] = 1 / t.visc_exponent[i] - 1;   // IEEE division: same bits as per element
+        t.visc_pw1[i] = -1 / t.visc_exponent[i];
+        t.pt_phi[2 * i] = t.friction_angle0[i];
+        t.pt_psi[2 * i] = t.dilation_angle0[i];
+        t.pt_phi[2 * i + 1] = t.friction_angle1[i];
+        t.pt_psi[2 * i + 1] = t.dilation_angle1[i];
+    }
+    t.pt_n = 0;   // enabled once the device has filled the table
+    t.hr_over_cp = t.radiogenic_heating[0] / t.heat_capacity[0];
     return DES_OK;
+}
+
+void set_rho_pseudo(des_ctx *c)
+{
+    const double ps = c->kp.prm.max_vbc_val * c->kp.prm.inertial_scaling;
+    c->kp.mat.rho_pseudo = c->kp.mat.bulk_modulus[0] / (ps * ps);
 }
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -146,7 +167,7 @@ size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 extern "C" {
 
-const char *des_version(void) { return "desgpu 0.1 (sm_103a, FP64 explicit step)"; }
+const char *des_version(void) { return "desgpu 0.2 (sm_103a; FP64 and mixed FP32/FP64 explicit step)"; }
 
 int des_last_error(const des_ctx *c, char *buf, size_t len)
 {
@@ -298,6 +319,9 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     add((void **)&p.vol, (size_t)ne * D);
     add((void **)&p.vol_old, (size_t)ne * D);
     add((void **)&p.shp, (size_t)ne * npe * nd * D);
+    const bool mixed3 = (precision == DES_PREC_MIXED) && nd == 3;
+    float *d_shp32 = nullptr;
+    if (mixed3) add((void **)&d_shp32, (size_t)ne * npe * nd * sizeof(float));
     add((void **)&c->d_rho, (size_t)ne * D);
     add((void **)&p.fv, (size_t)std::max(nbf, 1) * nd * D);
     add((void **)&p.clk, sizeof(Clock));
@@ -348,6 +372,7 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     p.emark = d_emark;
     p.rho_e = nullptr;
     p.tdot = p.ntmp;
+    p.shp32 = d_shp32;
     for (int i = 0; i < DES_NBDRYTYPES; ++i)
         for (int d = 0; d < 3; ++d) {
             p.bnormals[i][d] = mesh->bnormals[i][d];
@@ -381,6 +406,29 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
         Clock ck{};
         ck.red_minh = ck.red_maxwell = ck.red_diffusion = ~0ull;
         e1 = cudaMemcpy(p.clk, &ck, sizeof ck, cudaMemcpyHostToDevice);
+    }
+    if (e1 == cudaSuccess) {
+        // material constants computed by the device's own functions
+        set_rho_pseudo(c);
+        const int nm = p.mat.nmat;
+        std::vector<double> tab(nm + 8 * nm);
+        launch_material_table(p, c->stream, c->d_stage);
+        e1 = cudaMemcpyAsync(tab.data(), c->d_stage, tab.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                             c->stream);
+        if (e1 == cudaSuccess) e1 = cudaStreamSynchronize(c->stream);
+        if (e1 == cudaSuccess) {
+            for (int m = 0; m < nm; ++m) p.mat.visc_coef[m] = tab[m];
+            p.mat.visc_lnc = std::log(0.25e6 * tab[0]);
+            p.mat.visc_lnmin = std::log(p.mat.visc_min);
+            p.mat.visc_lnmax = std::log(p.mat.visc_max);
+            for (int k = 0; k < 2 * nm; ++k) {
+                p.mat.pt_anphi[k] = tab[nm + 4 * k + 0];
+                p.mat.pt_anpsi[k] = tab[nm + 4 * k + 1];
+                p.mat.pt_sqrt_anphi[k] = tab[nm + 4 * k + 2];
+                p.mat.pt_tanphi[k] = tab[nm + 4 * k + 3];
+            }
+            p.mat.pt_n = 2 * nm;
+        }
     }
     if (e1 != cudaSuccess) {
         int code = fail_msg(g_create_error, DES_ECUDA, "device setup: %s", cudaGetErrorString(e1));
@@ -623,10 +671,13 @@ int des_set_clock(des_ctx *c, double time, double dt, int steps)
     }
 
 PERFN(des_update_temperature, n += launch_heat_gather(p, s); n += launch_temperature_update(p, s))
-PERFN(des_update_strain_rate, n += launch_strain_rate(p, s, false))
+PERFN(des_update_strain_rate,
+      n += (p.shp32 ? launch_strain_rate_mixed(p, s, false) : launch_strain_rate(p, s, false)))
 PERFN(des_compute_dvoldt, n += launch_dvoldt(p, s))
 PERFN(des_compute_edvoldt, n += launch_edvoldt(p, s))
-PERFN(des_update_stress, n += launch_update_stress(p, s, false))
+PERFN(des_update_stress,
+      n += ((p.shp32 && !p.mat.is_plane_strain) ? launch_update_stress_mixed(p, s, false)
+                                                 : launch_update_stress(p, s, false)))
 PERFN(des_NMD_stress, n += launch_nmd_gather(p, s); n += launch_nmd_correct(p, s, false))
 PERFN(des_update_force, n += launch_facet_forces(p, s); n += launch_force(p, s, false))
 PERFN(des_update_velocity, n += launch_velocity(p, s))
@@ -636,7 +687,7 @@ PERFN(des_swap_volume, n += launch_geometry(p, s, GEO_COPY_OLD))
 PERFN(des_compute_volume, n += launch_geometry(p, s, GEO_VOLUME))
 PERFN(des_compute_mass, n += launch_mass(p, s))
 PERFN(des_compute_shape_fn, n += launch_geometry(p, s, GEO_SHAPE))
-PERFN(des_rotate_stress, n += launch_geometry(p, s, GEO_ROTATE))
+PERFN(des_rotate_stress, n += (p.shp32 ? launch_rotate_mixed(p, s) : launch_geometry(p, s, GEO_ROTATE)))
 PERFN(des_update_mesh, n += launch_coordinate(p, s);
       n += launch_geometry(p, s, GEO_COPY_OLD | GEO_VOLUME); n += launch_mass(p, s);
       n += launch_geometry(p, s, GEO_SHAPE))
@@ -678,8 +729,31 @@ int des_worst_elem_quality(des_ctx *c, double *quality, int *elem)
 // ---- the fused step ----
 namespace {
 
+bool use_mixed(const des_ctx *c) { return c->kp.shp32 != nullptr && !c->kp.mat.is_plane_strain; }
+
+int enqueue_step_mixed(des_ctx *c)
+{
+    const KP p = step_kp(c);
+    cudaStream_t s = c->stream;
+    int n = 0;
+    const bool thermal = p.prm.has_thermal_diffusion != 0;
+    n += launch_strain_rate_mixed(p, s, true);
+    n += launch_heat_and_dvoldt_mixed(p, s, thermal);
+    if (thermal) n += launch_temperature_update(p, s);
+    n += launch_update_stress_mixed(p, s, true);
+    n += launch_nmd_gather(p, s);
+    n += launch_nmd_correct(p, s, true);
+    n += launch_force(p, s, true);
+    n += launch_geometry(p, s, GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP);
+    if (p.mat.rheol_type & DES_RH_ELASTIC) n += launch_rotate_mixed(p, s);
+    n += launch_mass(p, s);
+    n += launch_dt_finalize(p, s, true);
+    return n;
+}
+
 int enqueue_step(des_ctx *c)
 {
+    if (use_mixed(c)) return enqueue_step_mixed(c);
     const KP p = step_kp(c);
     cudaStream_t s = c->stream;
     int n = 0;

@@ -55,6 +55,23 @@ struct MatC {
     double cohesion0[DES_MAXMAT], cohesion1[DES_MAXMAT];
     double friction_angle0[DES_MAXMAT], friction_angle1[DES_MAXMAT];
     double dilation_angle0[DES_MAXMAT], dilation_angle1[DES_MAXMAT];
+    // material constants hoisted out of the per-element work.  Each is
+    // computed once with the very operation the per-element code would
+    // perform on the same operands (on the device for the transcendental
+    // ones), so using it changes no bit of the result.
+    double visc_pw[DES_MAXMAT];      // 1 / n - 1               (matprops.cxx:298)
+    double visc_pw1[DES_MAXMAT];     // -1 / n                  (matprops.cxx:299)
+    double visc_coef[DES_MAXMAT];    // pow(0.75 * A, -1 / n)   (matprops.cxx:300)
+    double rho_pseudo;               // bulkm / (v_max * inertial_scaling)^2 (geometry.cxx:348-349), nmat == 1
+    double visc_lnc;                 // ln(0.25e6 * visc_coef[0])   (mixed step, nmat == 1)
+    double visc_lnmin, visc_lnmax;   // ln(visc_min), ln(visc_max)  (mixed step)
+    double hr_over_cp;               // hr / cp (fields.cxx:118), nmat == 1
+    // plastic_props at the material's start / saturated angles
+    // (matprops.cxx:365-372): entry 2m at (phi0, psi0), 2m+1 at (phi1, psi1)
+    int pt_n;
+    double pt_phi[2 * DES_MAXMAT], pt_psi[2 * DES_MAXMAT];
+    double pt_anphi[2 * DES_MAXMAT], pt_anpsi[2 * DES_MAXMAT];
+    double pt_sqrt_anphi[2 * DES_MAXMAT], pt_tanphi[2 * DES_MAXMAT];
 };
 
 // Everything a kernel needs, passed by value.
@@ -74,6 +91,7 @@ struct KP {
     double *rho_e;                       // per-element density of the step (scratch), or null
     double *tdot;                        // node scratch for the heat gather (ntmp outside the fused step)
     double *fv;                          // [nd][nbf] per-facet stress-BC force (scratch)
+    float *shp32;                        // FP32 copy of shp for the mixed step, or null
     const double *ef[DES_EF_COUNT];      // per-element overrides or null
     Clock *clk;
     unsigned *err;
@@ -207,9 +225,8 @@ __device__ double m_visc(const KP &p, int e, const double *edot)
         double result = 0;
         int n = 0;
         for (int m = 0; m < p.mat.nmat; m++) {
-            double pw = 1 / p.mat.visc_exponent[m] - 1;
-            double pw1 = -1 / p.mat.visc_exponent[m];
-            double visc0 = 0.25 * pow(ed, pw) * pow(0.75 * p.mat.visc_coefficient[m], pw1)
+            const double pw = p.mat.visc_pw[m];
+            const double visc0 = 0.25 * pow(ed, pw) * p.mat.visc_coef[m]
                 * exp(p.mat.visc_activation_energy[m] / (p.mat.visc_exponent[m] * gas_constant * T)) * 1e6;
             int k = mcount(p, e, m);
             result += k / visc0;
@@ -218,6 +235,17 @@ __device__ double m_visc(const KP &p, int e, const double *edot)
         v = n / result;
     }
     return dmin_(dmax_(v, p.mat.visc_min), p.mat.visc_max);
+}
+
+// angle-dependent part of plastic_props (matprops.cxx:365-372)
+__device__ inline void plastic_angles(double phi, double psi, double &anphi, double &anpsi, double &sq, double &tn)
+{
+    double sphi = sin(phi * DEG2RAD);
+    double spsi = sin(psi * DEG2RAD);
+    anphi = (1 + sphi) / (1 - sphi);
+    anpsi = (1 + spsi) / (1 - spsi);
+    sq = sqrt(anphi);
+    tn = tan(phi * DEG2RAD);
 }
 
 // MatProps::plastic_weakening + plastic_props (matprops.cxx:315-373)
@@ -256,12 +284,20 @@ __device__ inline void m_plastic_props(const KP &p, int e, double pls, double &a
     }
     double cohesion = cc / n, phi = f / n, psi = d / n;
     hardn = h / n;
-    double sphi = sin(phi * DEG2RAD);
-    double spsi = sin(psi * DEG2RAD);
-    anphi = (1 + sphi) / (1 - sphi);
-    anpsi = (1 + spsi) / (1 - spsi);
-    amc = 2 * cohesion * sqrt(anphi);
-    ten_max = (phi == 0) ? p.mat.tension_max : dmin_(p.mat.tension_max, cohesion / tan(phi * DEG2RAD));
+    int hit = -1;
+    for (int k = 0; k < p.mat.pt_n; ++k)
+        if (phi == p.mat.pt_phi[k] && psi == p.mat.pt_psi[k]) hit = k;
+    double sq, tn;
+    if (hit >= 0) {
+        anphi = p.mat.pt_anphi[hit];
+        anpsi = p.mat.pt_anpsi[hit];
+        sq = p.mat.pt_sqrt_anphi[hit];
+        tn = p.mat.pt_tanphi[hit];
+    } else {
+        plastic_angles(phi, psi, anphi, anpsi, sq, tn);
+    }
+    amc = 2 * cohesion * sq;
+    ten_max = (phi == 0) ? p.mat.tension_max : dmin_(p.mat.tension_max, cohesion / tn);
 }
 
 // ref_pressure option 0 (matprops.cxx:190-202)

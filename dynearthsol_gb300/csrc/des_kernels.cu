@@ -99,7 +99,7 @@ __device__ __forceinline__ double heat_term(const KP &p, int e, int i)
     constexpr int NPE = ND + 1;
     double vol = p.vol[e];
     double kv = m_k(p, e) * vol;
-    double rh = (m_hr(p, e) / m_cp(p, e)) * vol;
+    double rh = ((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * vol;
     double sxi = shp_at(p, 0, i, e), szi = shp_at(p, ND - 1, i, e);
     double syi = (ND == 3) ? shp_at(p, 1, i, e) : 0.0;
     double diffusion = 0;
@@ -674,6 +674,12 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
             for (int k = 0; k < ND; ++k)
 #pragma unroll
                 for (int i = 0; i < NPE; ++i) p.shp[((size_t)k * NPE + i) * ne + e] = shp[k][i];
+            if (p.shp32) {
+#pragma unroll
+                for (int k = 0; k < ND; ++k)
+#pragma unroll
+                    for (int i = 0; i < NPE; ++i) p.shp32[((size_t)k * NPE + i) * ne + e] = (float)shp[k][i];
+            }
         } else if (flags & GEO_ROTATE) {
 #pragma unroll
             for (int k = 0; k < ND; ++k)
@@ -797,7 +803,8 @@ __global__ void __launch_bounds__(TPB) k_mass(KP p)
         int e = p.sup_ent[q] >> 2;
         double vol = p.vol[e];
         double rho_e = p.rho_e ? p.rho_e[e] : m_rho<ND>(p, e);
-        double rho = quasi ? m_bulkm(p, e) / (pseudo_speed * pseudo_speed) : rho_e;
+        double rho = quasi ? ((p.mat.nmat == 1) ? p.mat.rho_pseudo : m_bulkm(p, e) / (pseudo_speed * pseudo_speed))
+                           : rho_e;
         double m = rho * vol / NPE;
         vn += vol;
         ms += m;
@@ -859,6 +866,31 @@ __global__ void __launch_bounds__(TPB) k_quality_arg(KP p, unsigned long long *r
     double q = elem_quality<ND>(p, e);
     unsigned long long b = q > 0 ? dbits(q) : 0ull;
     if (b == red[0]) atomicMin(&red[1], (unsigned long long)e);
+}
+
+// ==================================================================
+// material constants (see MatC): out[0..] = visc_coef[nmat], then for each
+// of the 2*nmat plastic table entries anphi, anpsi, sqrt(anphi), tan(phi)
+// ==================================================================
+__global__ void k_material_table(KP p, double *out)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const int nm = p.mat.nmat;
+    for (int m = 0; m < nm; ++m) out[m] = pow(0.75 * p.mat.visc_coefficient[m], p.mat.visc_pw1[m]);
+    for (int k = 0; k < 2 * nm; ++k) {
+        double an, ap, sq, tn;
+        plastic_angles(p.mat.pt_phi[k], p.mat.pt_psi[k], an, ap, sq, tn);
+        out[nm + 4 * k + 0] = an;
+        out[nm + 4 * k + 1] = ap;
+        out[nm + 4 * k + 2] = sq;
+        out[nm + 4 * k + 3] = tn;
+    }
+}
+
+int launch_material_table(const KP &p, cudaStream_t s, double *out)
+{
+    k_material_table<<<1, 1, 0, s>>>(p, out);
+    return 1;
 }
 
 // ==================================================================

@@ -37,6 +37,8 @@ int launch_mass(const KP &p, cudaStream_t s);
 int launch_dt_finalize(const KP &p, cudaStream_t s, bool only_on_step);
 int launch_quality(const KP &p, cudaStream_t s, unsigned long long *red);
 int launch_dt_reset(const KP &p, cudaStream_t s);
+// material constants: visc_coef[nmat], then 4 values per plastic table entry
+int launch_material_table(const KP &p, cudaStream_t s, double *out);
 
 // layout conversion between the reference's AoS rows and device SoA
 int launch_aos_to_soa(const double *aos, double *soa, int n, int ncomp, cudaStream_t s);

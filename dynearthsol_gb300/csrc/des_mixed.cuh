@@ -1,0 +1,15 @@
+// des_mixed.cuh -- launchers of the mixed-precision (DES_PREC_MIXED) kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "des_common.cuh"
+
+namespace des {
+
+int launch_update_stress_mixed(const KP &p, cudaStream_t s, bool fused);
+int launch_strain_rate_mixed(const KP &p, cudaStream_t s, bool begin_step);
+int launch_heat_and_dvoldt_mixed(const KP &p, cudaStream_t s, bool heat);
+int launch_rotate_mixed(const KP &p, cudaStream_t s);
+
+}  // namespace des

@@ -41,7 +41,7 @@ from cases import CASES, FUNCTIONS, PERFN_CASES, PERFN_MID_STEPS, build_case, re
 from dynearthsol_gb300.config import initial_state  # noqa: E402
 from oracle.oracle import Oracle, Reference, build_reference, state_copy  # noqa: E402
 
-ENVELOPE_FIELDS = ("vel", "stress", "temperature", "plstrain", "coord", "strain")
+ENVELOPE_FIELDS = ("vel", "stress", "temperature", "plstrain", "coord", "strain", "force")
 
 
 def envelope(wl, start, cp, clk, nsteps, result):

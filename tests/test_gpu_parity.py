@@ -82,7 +82,8 @@ def test_gpu_step_matches_reference(name):
         _cmp(out, g["final"], [k], max(TOL_STEP, ENV_MARGIN * env[k]), "final")
     others = [k for k in g["final"] if k in out and k not in KEY_FIELDS
               and not (wl.mesh.ndims == 2 and k == "shpdy")]
-    _cmp(out, g["final"], others, max(TOL_FIELD, ENV_MARGIN * env_max), "final")
+    for k in others:
+        _cmp(out, g["final"], [k], max(TOL_FIELD, ENV_MARGIN * env.get(k, env_max)), "final")
     t, dt, steps = m.clock()
     assert steps == int(g["final"]["clock"][2])
     assert abs(dt / g["final"]["clock"][1] - 1) < max(1e-9, ENV_MARGIN * env_max)
@@ -101,9 +102,11 @@ def test_gpu_steps_from_mid_state(name, k_steps, tol):
     m.step(k_steps)
     out = m.download()
     ref = g[f"mid{k_steps}"]
-    env = max(float(v) for v in g[f"envelope_mid{k_steps}"].values())
+    env = {k: float(v) for k, v in g[f"envelope_mid{k_steps}"].items()}
+    env_max = max(env.values())
     fields = [k for k in ref if k in out and k != "clock" and not (wl.mesh.ndims == 2 and k == "shpdy")]
-    _cmp(out, ref, fields, max(tol, ENV_MARGIN * env), f"mid+{k_steps}")
+    for k in fields:
+        _cmp(out, ref, [k], max(tol, ENV_MARGIN * env.get(k, env_max)), f"mid+{k_steps}")
 
 
 @pytest.mark.parametrize("name", PERFN_CASES)
@@ -234,12 +237,30 @@ def test_gpu_1000_steps_elastic_bit_exact_vs_oracle():
     assert max(errs.values()) == 0.0, errs
 
 
+def test_gpu_1000_steps_evp_damping2_vs_oracle():
+    """The 3D visco-elasto-plastic workload physics (weak zone yields) at
+    12x12x4 cubes with the continuous damping option 2: 1000 FP64 steps
+    within 1e-9 of the oracle on velocity, stress, temperature and plastic
+    strain.  With the default damping option 1 the reference's step is
+    chaotic (next test); with option 2 it is not, so this is the strict
+    long-run parity check of the whole path."""
+    from dataclasses import replace
+    from dynearthsol_gb300.config import make_workload
+    wl = make_workload("c1_3d_evp", cells=(12, 12, 4))
+    wl.params = replace(wl.params, damping_option=2)
+    errs, _ = _long_run(wl, 1000)
+    print("normalised errors after 1000 steps:", errs)
+    assert max(errs.values()) <= 1e-9, errs
+
+
 def test_gpu_1000_steps_evp_within_libm_envelope():
     """The 3D visco-elasto-plastic workload physics at 12x12x4 cubes, 1000
-    steps.  The reference's step is chaotic here (its min-J2 choice between
-    the Maxwell and elasto-plastic candidates and its copysign damping are
-    discontinuous), so the device is held to 20x the drift the oracle itself
-    shows when its libm results move by one ulp (two seeds, same run)."""
+    steps with the default damping option 1.  That damping,
+    f -= 0.8 copysign(f, v) for |v| > 1e-13 (fields.cxx:249-255), is
+    discontinuous in the sign of near-zero velocities, which makes the
+    reference's own run chaotic: a one-ulp change of its libm moves the
+    stress by ~1e-4 after 1000 steps.  The device is held to 20x the drift
+    the oracle shows under such a change (two seeds, same run)."""
     from dynearthsol_gb300.config import make_workload
     wl = make_workload("c1_3d_evp", cells=(12, 12, 4))
     errs, env = _long_run(wl, 1000, perturb_seeds=(1, 2))
