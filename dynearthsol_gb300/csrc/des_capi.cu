@@ -670,7 +670,9 @@ int des_set_clock(des_ctx *c, double time, double dt, int steps)
         return check_launch(c, n);            \
     }
 
-PERFN(des_update_temperature, n += launch_heat_gather(p, s); n += launch_temperature_update(p, s))
+PERFN(des_update_temperature,
+      n += (p.shp32 ? launch_heat_and_dvoldt_mixed(p, s, true, false) : launch_heat_gather(p, s));
+      n += launch_temperature_update(p, s))
 PERFN(des_update_strain_rate,
       n += (p.shp32 ? launch_strain_rate_mixed(p, s, false) : launch_strain_rate(p, s, false)))
 PERFN(des_compute_dvoldt, n += launch_dvoldt(p, s))
@@ -738,7 +740,7 @@ int enqueue_step_mixed(des_ctx *c)
     int n = 0;
     const bool thermal = p.prm.has_thermal_diffusion != 0;
     n += launch_strain_rate_mixed(p, s, true);
-    n += launch_heat_and_dvoldt_mixed(p, s, thermal);
+    n += launch_heat_and_dvoldt_mixed(p, s, thermal, true);
     if (thermal) n += launch_temperature_update(p, s);
     n += launch_update_stress_mixed(p, s, true);
     n += launch_nmd_gather(p, s);

@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(TPB_M) k_strain_rate_mixed3(KP p, int begin_st
 
 // heat stencil on FP64 temperature differences (sum_j D_ij = 0), FP32
 // products, FP64 nodal sum; dvoldt in FP64 (fields.cxx:99-146, geometry.cxx:111-155)
-__global__ void __launch_bounds__(TPB_M) k_heat_dvoldt_mixed3(KP p, int heat)
+__global__ void __launch_bounds__(TPB_M) k_heat_dvoldt_mixed3(KP p, int heat, int do_dvoldt)
 {
     int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= p.nn) return;
@@ -365,11 +365,13 @@ __global__ void __launch_bounds__(TPB_M) k_heat_dvoldt_mixed3(KP p, int heat)
             const double rh = ((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * vol;
             tdot += (double)((float)kv * diffusion) - rh;
         }
-        const double dj = p.srate[e] + p.srate[(size_t)p.ne + e] + p.srate[2 * (size_t)p.ne + e];
-        dvoldt += dj * vol;
+        if (do_dvoldt) {
+            const double dj = p.srate[e] + p.srate[(size_t)p.ne + e] + p.srate[2 * (size_t)p.ne + e];
+            dvoldt += dj * vol;
+        }
     }
     if (heat) p.tdot[n] = tdot;
-    p.ntmp[n] = dvoldt / p.vol_n[n];
+    if (do_dvoldt) p.ntmp[n] = dvoldt / p.vol_n[n];
 }
 
 // rotate_stress (fields.cxx:411-483) for the mixed step: spin from FP64
@@ -428,9 +430,9 @@ int launch_strain_rate_mixed(const KP &p, cudaStream_t s, bool begin_step)
     return 1;
 }
 
-int launch_heat_and_dvoldt_mixed(const KP &p, cudaStream_t s, bool heat)
+int launch_heat_and_dvoldt_mixed(const KP &p, cudaStream_t s, bool heat, bool dvoldt)
 {
-    k_heat_dvoldt_mixed3<<<nblocks_m(p.nn), TPB_M, 0, s>>>(p, (int)heat);
+    k_heat_dvoldt_mixed3<<<nblocks_m(p.nn), TPB_M, 0, s>>>(p, (int)heat, (int)dvoldt);
     return 1;
 }
 
