@@ -196,7 +196,9 @@ def run_reference(args, rank, world):
 
 
 def metric_name(args):
-    return "Mtet-steps/s"
+    if args.precision == "mixed":
+        return "Mtet-steps/s (mixed FP32/FP64 explicit step; FP64 step and stress error beside it)"
+    return "Mtet-steps/s (FP64 explicit step)"
 
 
 def config_of(args, wl):
@@ -206,16 +208,62 @@ def config_of(args, wl):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+def timed_steps(m, stream, steps, warmup, dist, sample_clocks=False, local=0):
+    """W untimed steps, then K steps between CUDA events on the library's
+    stream (barrier + synchronize on both sides); returns (ms, launches,
+    clocks)."""
+    import torch
+    m.step(warmup)
+    m.sync()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local) if sample_clocks else None
+    if sampler:
+        sampler.start()
+    l0 = m.launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    m.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop() if sampler else None
+    status = m.device_status()
+    if status:
+        raise RuntimeError(f"device status {status:#x} during the timed run")
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, m.launches() - l0, clocks
+
+
+def kernel_time(m, stream, fn, reps=20):
+    """Average duration (ms) of one per-function entry point, CUDA events."""
+    import torch
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    m.call(fn)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        m.call(fn)
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="c1_3d_evp")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true", help="skip the FP64 comparison run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -237,72 +285,55 @@ def main():
     from dynearthsol_gb300.solver import DeviceModel
 
     wl, st0, cp = setup_workload(args.workload)
-    prec = capi.PREC_FP64 if args.precision == "fp64" else capi.PREC_MIXED
-    stream = torch.cuda.Stream()
-    m = DeviceModel(wl, comp_pressure=cp, precision=prec, stream=stream.cuda_stream)
-    init = m.init_fields(st0)
-    clock0 = m.clock()
-
-    # ---- device-resident throughput ----
-    m.step(args.warmup)
-    m.sync()
-    if dist:
-        dist.barrier()
-    sampler = ClockSampler(local)
-    sampler.start()
-    l0 = m.launches()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    m.step(args.steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    launches = m.launches() - l0
-    clocks = sampler.stop()
-    status = m.device_status()
-    if status:
-        raise RuntimeError(f"device status {status:#x} during the timed run")
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
     ne, nn = wl.mesh.nelem, wl.mesh.nnode
-    value = world * ne * args.steps / (ms_max / 1e3) / 1e6
+    stream = torch.cuda.Stream()
+    f64 = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_FP64, stream=stream.cuda_stream)
+    init = f64.init_fields(st0)
+    clock0 = f64.clock()
+    if args.precision == "mixed":
+        m = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_MIXED, stream=stream.cuda_stream)
+        m.upload({k: v.copy() for k, v in init.items()}, clock0)
+    else:
+        m = f64
 
-    # ---- dominant kernel alone (update_stress) for the roofline ----
+    # ---- headline: device-resident throughput of the selected precision ----
+    ms, launches, clocks = timed_steps(m, stream, args.steps, args.warmup, dist, True, local)
+    value = world * ne * args.steps / (ms / 1e3) / 1e6
+    compare = None
+    if args.precision == "mixed" and not args.no_compare:
+        ms64, _, _ = timed_steps(f64, stream, args.steps, args.warmup, dist)
+        a, b = f64.download(), m.download()
+        l2 = float(np.linalg.norm(b["stress"] - a["stress"]) / np.linalg.norm(a["stress"]))
+        maxn = {k: float(np.abs(b[k] - a[k]).max() / max(np.abs(a[k]).max(), 1e-300))
+                for k in ("vel", "stress", "strain", "temperature", "plstrain", "coord", "force")}
+        compare = {"fp64_value": world * ne * args.steps / (ms64 / 1e3) / 1e6, "fp64_ms_per_step": ms64 / args.steps,
+                   "speedup_mixed_over_fp64": ms64 / ms,
+                   "stress_rel_l2_err_vs_fp64": l2, "gate": 1e-6,
+                   "steps_compared": args.warmup + args.steps,
+                   "max_normalised_err_vs_fp64": maxn}
+
+    # ---- dominant kernel alone, for the roofline ----
     m.upload(init, clock0)
     m.step(2)
-    ks0, ks1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 20
-    m.call("update_stress")
-    torch.cuda.synchronize()
-    ks0.record(stream)
-    for _ in range(reps):
-        m.call("update_stress")
-    ks1.record(stream)
-    torch.cuda.synchronize()
-    k_ms = ks0.elapsed_time(ks1) / reps
+    k_ms = kernel_time(m, stream, "update_stress")
     hbm_peak, peak_kind = measured_peaks()
     alg = STRESS_BYTES_PER_ELEM_FP64 * ne + 16 * nn
     achieved = alg / (k_ms / 1e3) / 1e9
-    traffic = profile_traffic("update_stress", args.workload)
-    roofline = {"bound": "hbm", "kernel": "k_update_stress", "achieved": achieved, "peak": hbm_peak,
-                "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                "kernel_ms": k_ms, "algorithmic_bytes_per_launch": alg,
-                "peak_kind": peak_kind,
-                "note": "FP64 update_stress is bound by the FP64 pipe (GB300 FP64 ~1/64 of FP32), not HBM"}
+    traffic = profile_traffic(f"update_stress_{args.precision}", args.workload)
+    roofline = {"bound": "hbm", "kernel": "k_update_stress" + ("_mixed3" if args.precision == "mixed" else "<3>"),
+                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": traffic, "kernel_ms": k_ms, "algorithmic_bytes_per_launch": alg,
+                "peak_kind": peak_kind}
     step_alg = step_bytes_per_tet(nn, ne)
-    step_gbs = step_alg * ne * args.steps / (ms_max / 1e3) / 1e9
+    step_gbs = step_alg * ne * args.steps / (ms / 1e3) / 1e9
 
-    # ---- end to end through the host-buffer drop-in call ----
     e2e = None
     if args.e2e_steps > 0:
         e2e = run_e2e(args, m, wl, init, clock0, world, dist)
     if rank == 0:
         line = {
             "metric": metric_name(args), "value": value, "unit": "Mtet-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (structured box mesh, seeded; no dataset)",
@@ -310,6 +341,7 @@ def main():
             "roofline": roofline,
             "step_hbm": {"algorithmic_bytes_per_tet": step_alg, "achieved_gbs": step_gbs,
                          "frac": step_gbs / hbm_peak},
+            "mixed_vs_fp64": compare,
             "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": clocks,
@@ -321,6 +353,7 @@ def main():
         dist.barrier()
         dist.destroy_process_group()
     m.close()
+    f64.close()
     return 0
 
 

@@ -45,6 +45,14 @@ EF_FRICTION1 = 5
 EF_THERM_COND = 6
 EF_COUNT = 7
 
+F_BITS = {name: 1 << i for i, name in enumerate(
+    ("coord", "coord0", "vel", "force", "temperature", "mass", "tmass", "volume_n", "ntmp", "volume",
+     "volume_old", "stress", "strain", "strain_rate", "plstrain", "delta_plstrain", "stressyy",
+     "dpressure", "edvoldt"))}
+F_SHP = 1 << 19
+F_CLOCK = 1 << 20
+F_ALL = (1 << 21) - 1
+
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _up = C.POINTER(C.c_uint)
@@ -169,6 +177,9 @@ _SIGS = {
     "des_upload_state": [C.c_void_p, C.POINTER(DesHostState)],
     "des_download_state": [C.c_void_p, C.POINTER(DesHostState)],
     "des_set_params": [C.c_void_p, C.POINTER(DesParams)],
+    "des_upload_fields": [C.c_void_p, C.POINTER(DesHostState), C.c_uint],
+    "des_download_fields": [C.c_void_p, C.POINTER(DesHostState), C.c_uint],
+    "des_set_elemmarkers": [C.c_void_p, _ip],
     "des_set_elem_field": [C.c_void_p, C.c_int, _dp],
     "des_update_temperature": [C.c_void_p],
     "des_update_strain_rate": [C.c_void_p],

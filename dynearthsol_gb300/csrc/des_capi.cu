@@ -632,6 +632,142 @@ int des_download_state(des_ctx *c, des_host_state *st)
     return DES_OK;
 }
 
+namespace {
+
+struct FieldDesc {
+    unsigned bit;
+    double *des_host_state::*member;
+    int node;    // 1: node field, 0: element field
+    int ncomp;   // 0: nd, -1: nstr, -2: npe (shape functions), else the count
+};
+
+const FieldDesc kFields[] = {
+    {DES_F_COORD, &des_host_state::coord, 1, 0},
+    {DES_F_COORD0, &des_host_state::coord0, 1, 0},
+    {DES_F_VEL, &des_host_state::vel, 1, 0},
+    {DES_F_FORCE, &des_host_state::force, 1, 0},
+    {DES_F_TEMPERATURE, &des_host_state::temperature, 1, 1},
+    {DES_F_MASS, &des_host_state::mass, 1, 1},
+    {DES_F_TMASS, &des_host_state::tmass, 1, 1},
+    {DES_F_VOLUME_N, &des_host_state::volume_n, 1, 1},
+    {DES_F_NTMP, &des_host_state::ntmp, 1, 1},
+    {DES_F_VOLUME, &des_host_state::volume, 0, 1},
+    {DES_F_VOLUME_OLD, &des_host_state::volume_old, 0, 1},
+    {DES_F_STRESS, &des_host_state::stress, 0, -1},
+    {DES_F_STRAIN, &des_host_state::strain, 0, -1},
+    {DES_F_STRAIN_RATE, &des_host_state::strain_rate, 0, -1},
+    {DES_F_PLSTRAIN, &des_host_state::plstrain, 0, 1},
+    {DES_F_DELTA_PLSTRAIN, &des_host_state::delta_plstrain, 0, 1},
+    {DES_F_STRESSYY, &des_host_state::stressyy, 0, 1},
+    {DES_F_DPRESSURE, &des_host_state::dpressure, 0, 1},
+    {DES_F_EDVOLDT, &des_host_state::edvoldt, 0, 1},
+};
+
+double *device_field(des_ctx *c, unsigned bit)
+{
+    KP &p = c->kp;
+    switch (bit) {
+    case DES_F_COORD: return p.x;
+    case DES_F_COORD0: return p.x0;
+    case DES_F_VEL: return p.v;
+    case DES_F_FORCE: return p.f;
+    case DES_F_TEMPERATURE: return p.T;
+    case DES_F_MASS: return p.mass;
+    case DES_F_TMASS: return p.tmass;
+    case DES_F_VOLUME_N: return p.vol_n;
+    case DES_F_NTMP: return p.ntmp;
+    case DES_F_VOLUME: return p.vol;
+    case DES_F_VOLUME_OLD: return p.vol_old;
+    case DES_F_STRESS: return p.stress;
+    case DES_F_STRAIN: return p.strain;
+    case DES_F_STRAIN_RATE: return p.srate;
+    case DES_F_PLSTRAIN: return p.pls;
+    case DES_F_DELTA_PLSTRAIN: return p.dpls;
+    case DES_F_STRESSYY: return p.syy;
+    case DES_F_DPRESSURE: return p.dp;
+    case DES_F_EDVOLDT: return p.edvoldt;
+    default: return nullptr;
+    }
+}
+
+int transfer_fields(des_ctx *c, des_host_state *st, unsigned mask, bool up)
+{
+    if (!c || !st) return DES_EINPUT;
+    if (mask & ~DES_F_ALL) return fail_msg(c->err, DES_EINPUT, "unknown field bits %#x", mask & ~DES_F_ALL);
+    int rc;
+    for (const FieldDesc &fd : kFields) {
+        if (!(mask & fd.bit)) continue;
+        double *h = st->*fd.member;
+        if (!h) return fail_msg(c->err, DES_EINPUT, "field %#x selected but NULL", fd.bit);
+        const int n = fd.node ? c->nn : c->ne;
+        const int k = fd.ncomp == 0 ? c->nd : (fd.ncomp == -1 ? c->nstr : fd.ncomp);
+        double *d = device_field(c, fd.bit);
+        rc = up ? put_field(c, h, d, n, k) : get_field(c, h, d, n, k);
+        if (rc) return rc;
+    }
+    if (mask & DES_F_SHP) {
+        double *arr[3] = {st->shpdx, c->nd == 3 ? st->shpdy : nullptr, st->shpdz};
+        int slot = 0;
+        for (int a = 0; a < 3; ++a) {
+            if (a == 1 && c->nd == 2) continue;
+            if (!arr[a]) return fail_msg(c->err, DES_EINPUT, "shape function array NULL");
+            double *d = c->kp.shp + (size_t)slot * c->ne * c->npe;
+            rc = up ? put_field(c, arr[a], d, c->ne, c->npe) : get_field(c, arr[a], d, c->ne, c->npe);
+            if (rc) return rc;
+            ++slot;
+        }
+        if (up && c->kp.shp32) {   // keep the FP32 copy of the mixed step in step
+            rc = check_launch(c, launch_geometry(c->kp, c->stream, GEO_SHAPE));
+            if (rc) return rc;
+        }
+    }
+    if (mask & DES_F_CLOCK) {
+        Clock ck;
+        CK(cudaMemcpyAsync(&ck, c->kp.clk, sizeof ck, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        if (up) {
+            ck.time = st->time;
+            ck.dt = st->dt;
+            ck.steps = st->steps;
+            CK(cudaMemcpyAsync(c->kp.clk, &ck, sizeof ck, cudaMemcpyHostToDevice, c->stream));
+        } else {
+            st->time = ck.time;
+            st->dt = ck.dt;
+            st->steps = ck.steps;
+        }
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return DES_OK;
+}
+
+}  // namespace
+
+int des_upload_fields(des_ctx *c, const des_host_state *st, unsigned mask)
+{
+    int rc = transfer_fields(c, const_cast<des_host_state *>(st), mask, true);
+    if (rc == DES_OK) c->has_state = true;
+    return rc;
+}
+
+int des_download_fields(des_ctx *c, des_host_state *st, unsigned mask)
+{
+    return transfer_fields(c, st, mask, false);
+}
+
+int des_set_elemmarkers(des_ctx *c, const int *em)
+{
+    if (!c || !em) return DES_EINPUT;
+    if (!c->kp.emark) return fail_msg(c->err, DES_EINPUT, "context was created without per-element markers");
+    const int nm = c->kp.mat.nmat, ne = c->ne;
+    std::vector<int> soa((size_t)ne * nm);
+    for (int e = 0; e < ne; ++e)
+        for (int m = 0; m < nm; ++m) soa[(size_t)m * ne + e] = em[(size_t)e * nm + m];
+    CK(cudaMemcpyAsync(const_cast<int *>(c->kp.emark), soa.data(), soa.size() * sizeof(int),
+                       cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return DES_OK;
+}
+
 int des_get_clock(des_ctx *c, double *time, double *dt, int *steps)
 {
     if (!c) return DES_EINPUT;

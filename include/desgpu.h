@@ -183,6 +183,40 @@ int des_device_status(des_ctx *ctx, unsigned *bits);
 int des_upload_state(des_ctx *ctx, const des_host_state *st);
 int des_download_state(des_ctx *ctx, des_host_state *st);
 
+/* Field-wise transfer: one bit per des_host_state array (DES_F_*), plus
+ * DES_F_CLOCK for time/dt/steps.  Only the selected fields move; a selected
+ * field whose pointer is NULL is an input error.  Used by a host shim that
+ * keeps the reference's Variables authoritative around each call. */
+#define DES_F_COORD          (1u << 0)
+#define DES_F_COORD0         (1u << 1)
+#define DES_F_VEL            (1u << 2)
+#define DES_F_FORCE          (1u << 3)
+#define DES_F_TEMPERATURE    (1u << 4)
+#define DES_F_MASS           (1u << 5)
+#define DES_F_TMASS          (1u << 6)
+#define DES_F_VOLUME_N       (1u << 7)
+#define DES_F_NTMP           (1u << 8)
+#define DES_F_VOLUME         (1u << 9)
+#define DES_F_VOLUME_OLD     (1u << 10)
+#define DES_F_STRESS         (1u << 11)
+#define DES_F_STRAIN         (1u << 12)
+#define DES_F_STRAIN_RATE    (1u << 13)
+#define DES_F_PLSTRAIN       (1u << 14)
+#define DES_F_DELTA_PLSTRAIN (1u << 15)
+#define DES_F_STRESSYY       (1u << 16)
+#define DES_F_DPRESSURE      (1u << 17)
+#define DES_F_EDVOLDT        (1u << 18)
+#define DES_F_SHP            (1u << 19)   /* shpdx, shpdy (3D), shpdz */
+#define DES_F_CLOCK          (1u << 20)
+#define DES_F_ALL            ((1u << 21) - 1)
+int des_upload_fields(des_ctx *ctx, const des_host_state *st, unsigned mask);
+int des_download_fields(des_ctx *ctx, des_host_state *st, unsigned mask);
+
+/* Replace the per-element marker counts of a multi-material context
+ * ([nelem][nmat], Variables::elemmarkers), e.g. after phase changes
+ * (phasechanges.cxx:232-258) or marker remapping. */
+int des_set_elemmarkers(des_ctx *ctx, const int *elemmarkers);
+
 /* Replace the parameters (e.g. after a change of max_vbc_val). */
 int des_set_params(des_ctx *ctx, const des_params *param);
 
