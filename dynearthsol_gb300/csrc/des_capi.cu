@@ -579,6 +579,8 @@ int des_upload_state(des_ctx *c, const des_host_state *st)
         PUT(st->shpdx, p.shp, ne, npe);
         if (nd == 3) PUT(st->shpdy, p.shp + (size_t)ne * npe, ne, npe);
         PUT(st->shpdz, p.shp + (size_t)(nd - 1) * ne * npe, ne, npe);
+        if (p.shp32 && (rc = check_launch(c, launch_f64_to_f32(p.shp, p.shp32, (long long)ne * npe * nd, c->stream))))
+            return rc;
     } else if ((rc = check_launch(c, launch_geometry(q, c->stream, GEO_SHAPE)))) return rc;
     if (st->mass && st->tmass && st->volume_n) {
         PUT(st->mass, p.mass, nn, 1);
@@ -717,7 +719,8 @@ int transfer_fields(des_ctx *c, des_host_state *st, unsigned mask, bool up)
             ++slot;
         }
         if (up && c->kp.shp32) {   // keep the FP32 copy of the mixed step in step
-            rc = check_launch(c, launch_geometry(c->kp, c->stream, GEO_SHAPE));
+            rc = check_launch(c, launch_f64_to_f32(c->kp.shp, c->kp.shp32, (long long)c->ne * c->npe * c->nd,
+                                                   c->stream));
             if (rc) return rc;
         }
     }

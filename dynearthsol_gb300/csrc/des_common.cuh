@@ -193,6 +193,8 @@ __device__ __forceinline__ double m_rho_T(const KP &p, int e, double T)
 {
     const double celsius0 = 273;
     double TinCelsius = T - celsius0;
+    // one material, one marker: (x * 1) / 1 == x exactly
+    if (p.mat.nmat == 1 && !p.emark) return p.mat.rho0[0] * (1 - p.mat.alpha[0] * TinCelsius);
     double result = 0;
     int n = 0;
     for (int m = 0; m < p.mat.nmat; m++) {

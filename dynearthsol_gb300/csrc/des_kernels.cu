@@ -1042,6 +1042,18 @@ int launch_quality(const KP &p, cudaStream_t s, unsigned long long *red)
     return 2;
 }
 
+__global__ void k_f64_to_f32(const double *__restrict__ a, float *__restrict__ b, long long n)
+{
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+int launch_f64_to_f32(const double *a, float *b, long long n, cudaStream_t s)
+{
+    k_f64_to_f32<<<nblocks(n), TPB, 0, s>>>(a, b, n);
+    return 1;
+}
+
 int launch_aos_to_soa(const double *aos, double *soa, int n, int ncomp, cudaStream_t s)
 {
     k_aos_to_soa<<<nblocks((long long)n * ncomp), TPB, 0, s>>>(aos, soa, n, ncomp);

@@ -40,6 +40,9 @@ int launch_dt_reset(const KP &p, cudaStream_t s);
 // material constants: visc_coef[nmat], then 4 values per plastic table entry
 int launch_material_table(const KP &p, cudaStream_t s, double *out);
 
+// FP32 copy of an FP64 array (the mixed step's shape functions)
+int launch_f64_to_f32(const double *a, float *b, long long n, cudaStream_t s);
+
 // layout conversion between the reference's AoS rows and device SoA
 int launch_aos_to_soa(const double *aos, double *soa, int n, int ncomp, cudaStream_t s);
 int launch_soa_to_aos(const double *soa, double *aos, int n, int ncomp, cudaStream_t s);

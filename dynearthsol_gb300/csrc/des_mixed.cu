@@ -51,11 +51,13 @@ __device__ __forceinline__ void jrot(float (&a)[3][3], float (&v)[3][3])
     constexpr int R = 3 - P - Q;
     const float apq = a[P][Q];
     if (apq == 0.0f) return;
-    const float theta = (a[Q][Q] - a[P][P]) / (2.0f * apq);
-    const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.0f)));
+    const float theta = __fdividef(a[Q][Q] - a[P][P], 2.0f * apq);
+    // |theta| -> inf (negligible apq) gives t = 0: no rotation
+    const float at = fabsf(theta);
+    const float t = copysignf(__frcp_rn(at + __fsqrt_rn(fmaf(at, at, 1.0f))), theta);
     const float c = rsqrtf(fmaf(t, t, 1.0f));
     const float s = t * c;
-    const float tau = s / (1.0f + c);
+    const float tau = __fdividef(s, 1.0f + c);
     a[P][P] -= t * apq;
     a[Q][Q] += t * apq;
     a[P][Q] = a[Q][P] = 0.0f;
@@ -79,7 +81,7 @@ __device__ __forceinline__ void jacobi3f(const float d[6], float w[3], float (&v
 #pragma unroll
         for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? 1.0f : 0.0f;
 #pragma unroll
-    for (int sweep = 0; sweep < 5; ++sweep) {
+    for (int sweep = 0; sweep < 4; ++sweep) {
         jrot<0, 1>(a, v);
         jrot<0, 2>(a, v);
         jrot<1, 2>(a, v);
@@ -193,6 +195,15 @@ __device__ __forceinline__ unsigned elasto_plastic_mixed(double bulkm, double sh
     return 0;
 }
 
+// second invariant^2 of the deviator (utils.hpp:110-120) with the mean
+// formed by a multiplication (the mixed step needs no bit parity)
+__device__ __forceinline__ double j2_mixed(const double *t)
+{
+    double a = (t[0] + t[1] + t[2]) * (1.0 / 3);
+    return (0.5 * ((t[0] - a) * (t[0] - a) + (t[1] - a) * (t[1] - a) + (t[2] - a) * (t[2] - a))
+            + t[3] * t[3] + t[4] * t[4] + t[5] * t[5]);
+}
+
 // update_stress (rheology.cxx:510-646), 3D, mixed precision
 __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
 {
@@ -277,7 +288,7 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
 #pragma unroll
             for (int i = 0; i < 6; ++i) sv[i] = s[i];
             maxwell_mixed(bulkm, shearm, visc_mixed(p, e, edot, T), dt, dv, de, dev, sv);
-            const double svII = second_invariant2_<3>(sv), spII = second_invariant2_<3>(sp);
+            const double svII = j2_mixed(sv), spII = j2_mixed(sp);
             if (svII < spII) {
 #pragma unroll
                 for (int i = 0; i < 6; ++i) s[i] = sv[i];
