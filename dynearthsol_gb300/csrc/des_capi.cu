@@ -421,6 +421,7 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
             p.mat.visc_lnc = std::log(0.25e6 * tab[0]);
             p.mat.visc_lnmin = std::log(p.mat.visc_min);
             p.mat.visc_lnmax = std::log(p.mat.visc_max);
+            p.mat.visc_qnr = p.mat.visc_activation_energy[0] / (p.mat.visc_exponent[0] * 8.3144);
             for (int k = 0; k < 2 * nm; ++k) {
                 p.mat.pt_anphi[k] = tab[nm + 4 * k + 0];
                 p.mat.pt_anpsi[k] = tab[nm + 4 * k + 1];

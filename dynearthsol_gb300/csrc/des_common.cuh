@@ -65,6 +65,7 @@ struct MatC {
     double rho_pseudo;               // bulkm / (v_max * inertial_scaling)^2 (geometry.cxx:348-349), nmat == 1
     double visc_lnc;                 // ln(0.25e6 * visc_coef[0])   (mixed step, nmat == 1)
     double visc_lnmin, visc_lnmax;   // ln(visc_min), ln(visc_max)  (mixed step)
+    double visc_qnr;                 // Q / (n R)                   (mixed step)
     double hr_over_cp;               // hr / cp (fields.cxx:118), nmat == 1
     // plastic_props at the material's start / saturated angles
     // (matprops.cxx:365-372): entry 2m at (phi0, psi0), 2m+1 at (phi1, psi1)

@@ -106,25 +106,35 @@ __device__ __forceinline__ void jacobi3f(const float d[6], float w[3], float (&v
     }
 }
 
-// Arrhenius power-law viscosity (matprops.cxx:276-312) for nmat == 1 in FP32
-// log form: ln visc = ln(0.25e6 * coef) + pw ln(edot_II) + Q / (n R T).
+// Arrhenius power-law viscosity (matprops.cxx:276-312) for nmat == 1:
+//   ln visc = ln(0.25e6 coef) + pw ln(edot_II) + Q / (n R T),
+// with every term kept to ~1e-8 absolute at ~10 FP64 operations:
+// ln(edot_II) = logf(mantissa) + exponent ln 2 (the FP32 log only sees
+// [0.5, 1)); 1/T from an FP32 seed and one FP64 Newton step; exp(ln visc) =
+// 2^k expf(r) with |r| <= ln2/2; the clamps to [visc_min, visc_max] are
+// exact.  The resulting viscosity is within ~2e-7 of the FP64 law.
 __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *edot, double T)
 {
     if (p.mat.nmat != 1 || p.ef[DES_EF_LOG10_VISC]) return m_visc<3>(p, e, edot);
+    const double LN2 = 0.6931471805599453, INV_LN2 = 1.4426950408889634;
     float t[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) t[i] = (float)edot[i];
-    float a = (t[0] + t[1] + t[2]) * (1.0f / 3.0f);
-    float j2 = 0.5f * ((t[0] - a) * (t[0] - a) + (t[1] - a) * (t[1] - a) + (t[2] - a) * (t[2] - a))
+    const float a = (t[0] + t[1] + t[2]) * (1.0f / 3.0f);
+    const float j2 = 0.5f * ((t[0] - a) * (t[0] - a) + (t[1] - a) * (t[1] - a) + (t[2] - a) * (t[2] - a))
         + t[3] * t[3] + t[4] * t[4] + t[5] * t[5];
-    float ed = fmaxf(sqrtf(j2), 1e-30f);
-    const double gas_constant = 8.3144;
-    float lnv = (float)p.mat.visc_lnc + (float)p.mat.visc_pw[0] * logf(ed)
-        + (float)(p.mat.visc_activation_energy[0] / (p.mat.visc_exponent[0] * gas_constant)) / (float)T;
-    // clamp in log space, then one exp (matprops.cxx:309)
-    lnv = fminf(fmaxf(lnv, (float)p.mat.visc_lnmin), (float)p.mat.visc_lnmax);
-    double v = (double)expf(lnv);
-    return dmin_(dmax_(v, p.mat.visc_min), p.mat.visc_max);
+    const float ed = fmaxf(sqrtf(j2), 1e-30f);
+    int ex;
+    const float mant = frexpf(ed, &ex);
+    const double ln_ed = (double)logf(mant) + (double)ex * LN2;
+    double r = (double)(1.0f / (float)T);
+    r = r * (2.0 - T * r);
+    const double lnv = p.mat.visc_lnc + p.mat.visc_pw[0] * ln_ed + p.mat.visc_qnr * r;
+    if (lnv <= p.mat.visc_lnmin) return p.mat.visc_min;
+    if (lnv >= p.mat.visc_lnmax) return p.mat.visc_max;
+    const double k = rint(lnv * INV_LN2);
+    const float rr = (float)(lnv - k * LN2);
+    return ldexp((double)expf(rr), (int)k);
 }
 
 // Maxwell update (rheology.cxx:118-134) in increment form:
