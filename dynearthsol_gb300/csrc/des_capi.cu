@@ -428,6 +428,12 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
                 p.mat.pt_sqrt_anphi[k] = tab[nm + 4 * k + 2];
                 p.mat.pt_tanphi[k] = tab[nm + 4 * k + 3];
             }
+            for (int m = 0; m < nm; ++m) {
+                // IEEE division: the same bits the per-element code computes
+                p.mat.pt_coh_over_tan[2 * m] = p.mat.cohesion0[m] / p.mat.pt_tanphi[2 * m];
+                p.mat.pt_coh_over_tan[2 * m + 1] = p.mat.cohesion1[m] / p.mat.pt_tanphi[2 * m + 1];
+                p.mat.hardening[m] = (p.mat.cohesion1[m] - p.mat.cohesion0[m]) / (p.mat.pls1[m] - p.mat.pls0[m]);
+            }
             p.mat.pt_n = 2 * nm;
         }
     }

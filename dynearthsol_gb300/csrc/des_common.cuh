@@ -73,6 +73,8 @@ struct MatC {
     double pt_phi[2 * DES_MAXMAT], pt_psi[2 * DES_MAXMAT];
     double pt_anphi[2 * DES_MAXMAT], pt_anpsi[2 * DES_MAXMAT];
     double pt_sqrt_anphi[2 * DES_MAXMAT], pt_tanphi[2 * DES_MAXMAT];
+    double pt_coh_over_tan[2 * DES_MAXMAT];   // cohesion0 / tan(phi0), cohesion1 / tan(phi1)
+    double hardening[DES_MAXMAT];             // (cohesion1 - cohesion0) / (pls1 - pls0)
 };
 
 // Everything a kernel needs, passed by value.
@@ -255,6 +257,51 @@ __device__ inline void plastic_angles(double phi, double psi, double &anphi, dou
 __device__ inline void m_plastic_props(const KP &p, int e, double pls, double &amc, double &anphi,
                                 double &anpsi, double &hardn, double &ten_max)
 {
+    if (p.mat.nmat == 1 && !p.emark && !p.ef[DES_EF_FRICTION0] && !p.ef[DES_EF_FRICTION1] && p.mat.pt_n >= 2) {
+        // One material, one marker: the marker-weighted sums and the
+        // divisions by the marker count are exact identities (0 + x*1 = x,
+        // x / 1 = x), and at the start / saturated angles the angle terms
+        // are the table entries, so this branch returns the very bits of
+        // the general loop below.
+        const double l0 = p.mat.pls0[0], l1 = p.mat.pls1[0];
+        const bool cov = p.ef[DES_EF_COHESION0] || p.ef[DES_EF_COHESION1];
+        const double c0 = p.ef[DES_EF_COHESION0] ? p.ef[DES_EF_COHESION0][e] : p.mat.cohesion0[0];
+        const double c1 = p.ef[DES_EF_COHESION1] ? p.ef[DES_EF_COHESION1][e] : p.mat.cohesion1[0];
+        int k;
+        double cohesion;
+        if (pls < l0) {
+            k = 0;
+            cohesion = c0;
+            hardn = 0;
+        } else if (pls < l1) {
+            hardn = cov ? (c1 - c0) / (l1 - l0) : p.mat.hardening[0];
+            if (pls == l0) {   // q = +0: c0 + 0*(c1-c0) == c0, phi0 + 0*(..) == phi0
+                k = 0;
+                cohesion = c0;
+            } else {
+                const double q = (pls - l0) / (l1 - l0);
+                cohesion = c0 + q * (c1 - c0);
+                const double phi = p.mat.friction_angle0[0] + q * (p.mat.friction_angle1[0] - p.mat.friction_angle0[0]);
+                const double psi = p.mat.dilation_angle0[0] + q * (p.mat.dilation_angle1[0] - p.mat.dilation_angle0[0]);
+                double sq, tn;
+                plastic_angles(phi, psi, anphi, anpsi, sq, tn);
+                amc = 2 * cohesion * sq;
+                ten_max = (phi == 0) ? p.mat.tension_max : dmin_(p.mat.tension_max, cohesion / tn);
+                return;
+            }
+        } else {
+            k = 1;
+            cohesion = c1;
+            hardn = 0;
+        }
+        anphi = p.mat.pt_anphi[k];
+        anpsi = p.mat.pt_anpsi[k];
+        amc = 2 * cohesion * p.mat.pt_sqrt_anphi[k];
+        const double phi = p.mat.pt_phi[k];
+        ten_max = (phi == 0) ? p.mat.tension_max
+                             : dmin_(p.mat.tension_max, cov ? cohesion / p.mat.pt_tanphi[k] : p.mat.pt_coh_over_tan[k]);
+        return;
+    }
     double cc = 0, f = 0, d = 0, h = 0;
     int n = 0;
     for (int m = 0; m < p.mat.nmat; m++) {

@@ -255,6 +255,7 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
     const float dev = (de[0] + de[1] + de[2]) * (1.0f / 3.0f);
     const int rt = p.mat.rheol_type;
     const double bulkm = m_bulkm(p, e), shearm = m_shearm(p, e);
+    const double T = elem_avg_T<4>(p, e);
     unsigned bits = 0;
     if (rt == DES_RH_ELASTIC) {
         const float lam = (float)(bulkm - 2. / 3 * shearm), g2 = (float)(2 * shearm);
@@ -264,10 +265,8 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
 #pragma unroll
         for (int i = 3; i < 6; ++i) s[i] += (double)(g2 * de[i]);
     } else if (rt == DES_RH_VISCOUS) {
-        const double T = elem_avg_T<4>(p, e);
         viscous_<3>(bulkm, visc_mixed(p, e, edot, T), es[0] + es[1] + es[2], edot, s);
     } else if (rt == DES_RH_MAXWELL) {
-        const double T = elem_avg_T<4>(p, e);
         const double vo = p.vol_old[e];
         const double dv = (double)((float)(p.vol[e] - vo) / (float)vo);
         maxwell_mixed(bulkm, shearm, visc_mixed(p, e, edot, T), dt, dv, de, dev, s);
@@ -291,7 +290,6 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
             pls += depls;
             dpls = depls;
         } else {   // EVP: the smaller second invariant wins (rheology.cxx:594-634)
-            const double T = elem_avg_T<4>(p, e);
             const double vo = p.vol_old[e];
             const double dv = (double)((float)(p.vol[e] - vo) / (float)vo);
             double sv[6];
@@ -319,7 +317,7 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
     p.pls[e] = pls;
     p.dpls[e] = dpls;
     p.dp[e] = (s[0] + s[1] + s[2]) - old_s;
-    if (fused && p.rho_e) p.rho_e[e] = m_rho<3>(p, e);
+    if (fused && p.rho_e) p.rho_e[e] = m_rho_T(p, e, T);
     if (bits) set_err(p, bits);
 }
 
