@@ -205,6 +205,7 @@ _SIGS = {
     "des_step_host": [C.c_void_p, C.POINTER(DesHostState), C.c_int],
     "des_synchronize": [C.c_void_p],
     "des_launch_count": [C.c_void_p, C.POINTER(C.c_longlong)],
+    "des_nmd_stress_noalloc": [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 8,
 }
 
 

@@ -275,6 +275,39 @@ int des_step(des_ctx *ctx, int nsteps);
  * This is the drop-in form for a caller whose Variables stay authoritative. */
 int des_step_host(des_ctx *ctx, des_host_state *st, int nsteps);
 
+/* ---- nodal-mixed pressure smoothing without any device allocation ---- */
+/* No counterpart in the reference: an extra entry point for callers that
+ * cannot allocate device memory -- a host application that owns every
+ * device byte and hands out memory only from its own pools, a process under
+ * a strict device-memory quota, or code running where cudaMalloc is not
+ * permitted (for example while another component holds the allocator).
+ * Such callers cannot use des_create, which allocates.
+ *
+ * It computes what des_NMD_stress computes (NMD_stress, geometry.cxx:
+ * 182-236) on arrays the caller already owns, all DEVICE pointers in the
+ * library's device layout: conn [ndims+1][nelem] (structure of arrays),
+ * support lists sup_off [nnode+1] and sup_ent (entries e*4 + local node,
+ * ascending element id per node), dpressure, volume [nelem], volume_n
+ * [nnode], and stress [nstr][nelem], whose first ndims components are
+ * updated in place.  Work is queued on stream (NULL: the legacy default
+ * stream).
+ *
+ * The per-node pressure sum it needs lives in a fixed device array of
+ * DES_NOALLOC_MAX_NODES doubles (16 MiB) that every GPU loading this library
+ * holds until the process exits; larger meshes are rejected with DES_EINPUT
+ * and a message on stderr.  The call makes no cudaMalloc, cudaFree or other
+ * allocating call.  All calls share that array and it keeps the last call's
+ * contents (each call overwrites every entry it reads, so nothing needs
+ * clearing); calls that overlap on the GPU (different streams, or different
+ * host threads) race on it and must be serialised by the caller.  The first
+ * call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. */
+#define DES_NOALLOC_MAX_NODES 2097152
+int des_nmd_stress_noalloc(int ndims, int nnode, int nelem, const int *conn, const int *sup_off,
+                           const int *sup_ent, const double *dpressure, const double *volume,
+                           const double *volume_n, double *stress, void *stream);
+
 /* Synchronise the context's stream. */
 int des_synchronize(des_ctx *ctx);
 
