@@ -835,7 +835,7 @@ PERFN(des_swap_volume, n += launch_geometry(p, s, GEO_COPY_OLD))
 PERFN(des_compute_volume, n += launch_geometry(p, s, GEO_VOLUME))
 PERFN(des_compute_mass, n += launch_mass(p, s))
 PERFN(des_compute_shape_fn, n += launch_geometry(p, s, GEO_SHAPE))
-PERFN(des_rotate_stress, n += (p.shp32 ? launch_rotate_mixed(p, s) : launch_geometry(p, s, GEO_ROTATE)))
+PERFN(des_rotate_stress, n += launch_geometry(p, s, GEO_ROTATE))
 PERFN(des_update_mesh, n += launch_coordinate(p, s);
       n += launch_geometry(p, s, GEO_COPY_OLD | GEO_VOLUME); n += launch_mass(p, s);
       n += launch_geometry(p, s, GEO_SHAPE))
@@ -892,8 +892,9 @@ int enqueue_step_mixed(des_ctx *c)
     n += launch_nmd_gather(p, s);
     n += launch_nmd_correct(p, s, true);
     n += launch_force(p, s, true);
-    n += launch_geometry(p, s, GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP);
-    if (p.mat.rheol_type & DES_RH_ELASTIC) n += launch_rotate_mixed(p, s);
+    int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP;
+    if (p.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;   // FP32 increments in a mixed context
+    n += launch_geometry(p, s, geo);
     n += launch_mass(p, s);
     n += launch_dt_finalize(p, s, true);
     return n;

@@ -566,12 +566,20 @@ __global__ void __launch_bounds__(TPB) k_coordinate(KP p)
 // element geometry: volume_old swap, compute_volume, compute_shape_fn,
 // rotate_stress, compute_dt element terms
 // ==================================================================
-template <int ND>
+// 1 / x from an FP32 seed and one FP64 Newton step (relative error ~1e-14),
+// for the mixed step only; the FP64 step divides
+__device__ __forceinline__ double recip_newton(double x)
+{
+    double r = (double)(1.0f / (float)x);
+    return r * (2.0 - x * r);
+}
+
+template <int ND, bool FAST_RECIP = false>
 __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], double vol, double (*shp)[ND + 1])
 {
     if (ND == 3) {
         const double *d0 = d[0], *d1 = d[1], *d2 = d[2], *d3 = d[3];
-        double iv = 1 / (6 * vol);
+        double iv = FAST_RECIP ? recip_newton(6 * vol) : 1 / (6 * vol);
         double x01 = d0[0] - d1[0], x02 = d0[0] - d2[0], x03 = d0[0] - d3[0];
         double x12 = d1[0] - d2[0], x13 = d1[0] - d3[0], x23 = d2[0] - d3[0];
         double y01 = d0[1] - d1[1], y02 = d0[1] - d2[1], y03 = d0[1] - d3[1];
@@ -592,7 +600,7 @@ __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], double vol,
         shp[ND - 1][3] = iv * (x01 * y02 - x02 * y01);
     } else {
         const double *d0 = d[0], *d1 = d[1], *d2 = d[2];
-        double iv = 1 / (2 * vol);
+        double iv = FAST_RECIP ? recip_newton(2 * vol) : 1 / (2 * vol);
         shp[0][0] = iv * (d1[1] - d2[1]);
         shp[0][1] = iv * (d2[1] - d0[1]);
         shp[0][2] = iv * (d0[1] - d1[1]);
@@ -669,7 +677,8 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
         }
         double shp[ND][NPE];
         if (flags & GEO_SHAPE) {
-            shape_fn_elem<ND>(c, vol, shp);
+            if (p.shp32) shape_fn_elem<ND, true>(c, vol, shp);
+            else shape_fn_elem<ND>(c, vol, shp);
 #pragma unroll
             for (int k = 0; k < ND; ++k)
 #pragma unroll
@@ -686,7 +695,44 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
 #pragma unroll
                 for (int i = 0; i < NPE; ++i) shp[k][i] = p.shp[((size_t)k * NPE + i) * ne + e];
         }
-        if (flags & GEO_ROTATE) {
+        if ((flags & GEO_ROTATE) && ND == 3 && p.shp32) {
+            // mixed step: spin from FP64 velocity differences, FP32 Jaumann
+            // increments added to the FP64 stress and strain
+            double v0[ND];
+            load_node_v<ND>(p, nodes[0], v0);
+            float w3 = 0, w4 = 0, w5 = 0;
+#pragma unroll
+            for (int i = 1; i < NPE; ++i) {
+                double vi[ND];
+                load_node_v<ND>(p, nodes[i], vi);
+                const float d0 = (float)(vi[0] - v0[0]), d1 = (float)(vi[1] - v0[1]), d2 = (float)(vi[ND - 1] - v0[ND - 1]);
+                const float sx = (float)shp[0][i], sy = (float)shp[1][i], sz = (float)shp[ND - 1][i];
+                w3 += 0.5f * (d0 * sy - d1 * sx);
+                w4 += 0.5f * (d0 * sz - d2 * sx);
+                w5 += 0.5f * (d1 * sz - d2 * sy);
+            }
+            const float dtf = (float)p.clk->dt;
+            double *arr[2] = {p.stress, p.strain};
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                double S[6];
+                float f[6];
+#pragma unroll
+                for (int cc = 0; cc < 6; ++cc) {
+                    S[cc] = arr[a][cc * ne + e];
+                    f[cc] = (float)S[cc];
+                }
+                float si[6];
+                si[0] = -2.0f * f[3] * w3 - 2.0f * f[4] * w4;
+                si[1] = 2.0f * f[3] * w3 - 2.0f * f[5] * w5;
+                si[2] = 2.0f * f[4] * w4 + 2.0f * f[5] * w5;
+                si[3] = f[0] * w3 - f[1] * w3 - f[4] * w5 - f[5] * w4;
+                si[4] = f[0] * w4 - f[2] * w4 + f[3] * w5 - f[5] * w3;
+                si[5] = f[1] * w5 - f[2] * w5 + f[3] * w4 + f[4] * w3;
+#pragma unroll
+                for (int cc = 0; cc < 6; ++cc) arr[a][cc * ne + e] = S[cc] + (double)(dtf * si[cc]);
+            }
+        } else if (flags & GEO_ROTATE) {
             double v[NPE][ND];
 #pragma unroll
             for (int i = 0; i < NPE; ++i) load_node_v<ND>(p, nodes[i], v[i]);

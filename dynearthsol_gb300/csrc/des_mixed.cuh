@@ -10,6 +10,5 @@ namespace des {
 int launch_update_stress_mixed(const KP &p, cudaStream_t s, bool fused);
 int launch_strain_rate_mixed(const KP &p, cudaStream_t s, bool begin_step);
 int launch_heat_and_dvoldt_mixed(const KP &p, cudaStream_t s, bool heat, bool dvoldt);
-int launch_rotate_mixed(const KP &p, cudaStream_t s);
 
 }  // namespace des
