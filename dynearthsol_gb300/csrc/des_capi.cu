@@ -320,8 +320,13 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     add((void **)&p.vol_old, (size_t)ne * D);
     add((void **)&p.shp, (size_t)ne * npe * nd * D);
     const bool mixed3 = (precision == DES_PREC_MIXED) && nd == 3;
-    float *d_shp32 = nullptr;
-    if (mixed3) add((void **)&d_shp32, (size_t)ne * npe * nd * sizeof(float));
+    float *d_shp32 = nullptr, *d_hc = nullptr;
+    double *d_qv = nullptr;
+    if (mixed3) {
+        add((void **)&d_shp32, (size_t)ne * npe * nd * sizeof(float));
+        add((void **)&d_hc, (size_t)ne * npe * sizeof(float));
+        add((void **)&d_qv, (size_t)ne * D);
+    }
     add((void **)&c->d_rho, (size_t)ne * D);
     add((void **)&p.fv, (size_t)std::max(nbf, 1) * nd * D);
     add((void **)&p.clk, sizeof(Clock));
@@ -373,6 +378,8 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     p.rho_e = nullptr;
     p.tdot = p.ntmp;
     p.shp32 = d_shp32;
+    p.hc = d_hc;
+    p.qv = d_qv;
     for (int i = 0; i < DES_NBDRYTYPES; ++i)
         for (int d = 0; d < 3; ++d) {
             p.bnormals[i][d] = mesh->bnormals[i][d];
@@ -885,9 +892,8 @@ int enqueue_step_mixed(des_ctx *c)
     cudaStream_t s = c->stream;
     int n = 0;
     const bool thermal = p.prm.has_thermal_diffusion != 0;
-    n += launch_strain_rate_mixed(p, s, true);
-    n += launch_heat_and_dvoldt_mixed(p, s, thermal, true);
-    if (thermal) n += launch_temperature_update(p, s);
+    n += launch_elem_pass_mixed(p, s, thermal);
+    n += launch_node_pass_mixed(p, s, thermal);
     n += launch_update_stress_mixed(p, s, true);
     n += launch_nmd_gather(p, s);
     n += launch_nmd_correct(p, s, true);

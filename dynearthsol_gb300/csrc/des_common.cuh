@@ -95,6 +95,8 @@ struct KP {
     double *tdot;                        // node scratch for the heat gather (ntmp outside the fused step)
     double *fv;                          // [nd][nbf] per-facet stress-BC force (scratch)
     float *shp32;                        // FP32 copy of shp for the mixed step, or null
+    float *hc;                           // [4][ne] per-element heat terms of the mixed step, or null
+    double *qv;                          // [ne] per-element dvoldt term of the mixed step, or null
     const double *ef[DES_EF_COUNT];      // per-element overrides or null
     Clock *clk;
     unsigned *err;
@@ -115,12 +117,47 @@ __device__ __forceinline__ double trace_(const double *s)
     return s[0] + s[1];
 }
 
+// x / 3 correctly rounded, with one multiplication and one fma instead of a
+// division (the method of Brisebarre, Muller and Raina, "Accelerating
+// correctly rounded floating-point division when the divisor is known in
+// advance", IEEE Trans. Computers 53(8), 2004).  With the two-term
+// reciprocal YH + YL of 3, fma(x, YH, x * YL) lies within ~1e-32 (relative)
+// of x / 3.  The exact quotient of a 53-bit significand by 3 has a
+// fractional part, in units of the quotient's last place, of 0, 1/3 or 2/3,
+// so it lies at least 1/6 ulp from every rounding midpoint, and the fma
+// rounds to the IEEE quotient: the result is bit-identical to x / 3.  Below
+// |x| = 2^-900, where x * YL could lose bits to underflow, it divides.
+__device__ __forceinline__ double div3(double x)
+{
+    constexpr double YH = 0x1.5555555555555p-2;    // RN(1/3)
+    constexpr double YL = 0x1.5555555555555p-56;   // RN(1/3 - YH)
+    if (fabs(x) < 0x1p-900) return x / 3;
+    return fma(x, YH, x * YL);
+}
+
+// x / ND for ND = 2 or 3, bit-identical to the division
+template <int ND>
+__device__ __forceinline__ double divnd(double x)
+{
+    if (ND == 3) return div3(x);
+    return x / ND;   // a power of two: the compiler multiplies by 0.5, exactly
+}
+
+// 1 / x from an FP32 seed and one FP64 Newton step (relative error ~1e-14,
+// for |x| within the FP32 normal range), for the mixed step only; the FP64
+// step divides
+__device__ __forceinline__ double recip_newton(double x)
+{
+    double r = (double)(1.0f / (float)x);
+    return r * (2.0 - x * r);
+}
+
 // utils.hpp:110-128
 template <int ND>
 __device__ __forceinline__ double second_invariant2_(const double *t)
 {
     if (ND == 3) {
-        double a = (t[0] + t[1] + t[2]) / 3;
+        double a = div3(t[0] + t[1] + t[2]);
         return (0.5 * ((t[0] - a) * (t[0] - a) + (t[1] - a) * (t[1] - a) + (t[2] - a) * (t[2] - a))
                 + t[3] * t[3] + t[4] * t[4] + t[5] * t[5]);
     }

@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(TPB) k_nmd_correct(KP p, int with_facets)
         double dp_el = dpn / (ND + 1);
         double dp_orig = p.dp[e];
 #pragma unroll
-        for (int i = 0; i < ND; ++i) p.stress[(size_t)i * p.ne + e] += (-dp_orig + dp_el) / ND;
+        for (int i = 0; i < ND; ++i) p.stress[(size_t)i * p.ne + e] += divnd<ND>(-dp_orig + dp_el);
     } else if (with_facets && t < p.ne + p.nbf) {
         facet_force<ND>(p, t - p.ne);
     }
@@ -566,14 +566,6 @@ __global__ void __launch_bounds__(TPB) k_coordinate(KP p)
 // element geometry: volume_old swap, compute_volume, compute_shape_fn,
 // rotate_stress, compute_dt element terms
 // ==================================================================
-// 1 / x from an FP32 seed and one FP64 Newton step (relative error ~1e-14),
-// for the mixed step only; the FP64 step divides
-__device__ __forceinline__ double recip_newton(double x)
-{
-    double r = (double)(1.0f / (float)x);
-    return r * (2.0 - x * r);
-}
-
 template <int ND, bool FAST_RECIP = false>
 __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], double vol, double (*shp)[ND + 1])
 {
@@ -716,19 +708,20 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
 #pragma unroll
             for (int a = 0; a < 2; ++a) {
                 double S[6];
-                float f[6];
 #pragma unroll
-                for (int cc = 0; cc < 6; ++cc) {
-                    S[cc] = arr[a][cc * ne + e];
-                    f[cc] = (float)S[cc];
-                }
+                for (int cc = 0; cc < 6; ++cc) S[cc] = arr[a][cc * ne + e];
+                // the isotropic part does not rotate: the normal-stress
+                // differences are taken in FP64, so the pressure never
+                // enters the FP32 products
+                const float d01 = (float)(S[0] - S[1]), d02 = (float)(S[0] - S[2]), d12 = (float)(S[1] - S[2]);
+                const float f3 = (float)S[3], f4 = (float)S[4], f5 = (float)S[5];
                 float si[6];
-                si[0] = -2.0f * f[3] * w3 - 2.0f * f[4] * w4;
-                si[1] = 2.0f * f[3] * w3 - 2.0f * f[5] * w5;
-                si[2] = 2.0f * f[4] * w4 + 2.0f * f[5] * w5;
-                si[3] = f[0] * w3 - f[1] * w3 - f[4] * w5 - f[5] * w4;
-                si[4] = f[0] * w4 - f[2] * w4 + f[3] * w5 - f[5] * w3;
-                si[5] = f[1] * w5 - f[2] * w5 + f[3] * w4 + f[4] * w3;
+                si[0] = -2.0f * f3 * w3 - 2.0f * f4 * w4;
+                si[1] = 2.0f * f3 * w3 - 2.0f * f5 * w5;
+                si[2] = 2.0f * f4 * w4 + 2.0f * f5 * w5;
+                si[3] = d01 * w3 - f4 * w5 - f5 * w4;
+                si[4] = d02 * w4 + f3 * w5 - f5 * w3;
+                si[5] = d12 * w5 + f3 * w4 + f4 * w3;
 #pragma unroll
                 for (int cc = 0; cc < 6; ++cc) arr[a][cc * ne + e] = S[cc] + (double)(dtf * si[cc]);
             }

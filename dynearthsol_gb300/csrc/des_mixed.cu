@@ -8,15 +8,16 @@
 //
 // * the viscosity (Arrhenius power law: pow, exp), evaluated to ~2e-7 with
 //   FP32 transcendentals on an exact exponent split (visc_mixed);
-// * the Mohr-Coulomb return map's eigen-solve: the DEVIATORIC trial stress
-//   is diagonalised in FP32 (branch-free cyclic Jacobi); the principal
-//   stresses, yield functions and plastic multiplier are formed in FP64 and
-//   the correction -alam * sum_k c_k v_k v_k^T (FP32 tensor, FP64 scale and
-//   sum) is applied to the FP64 trial stress;
-// * strain rate, spin and the heat stencil: sums of products of shape
-//   function derivatives with nodal values whose sum over the element
-//   vanishes, evaluated in FP32 on FP64 differences (v_i - v_0, T_j - T_i)
-//   so that nothing cancels in FP32; the Jaumann rotation increments.
+// * the Mohr-Coulomb yield test: the DEVIATORIC trial stress is
+//   diagonalised in FP32 (branch-free cyclic Jacobi) to screen out the
+//   elements that are elastic by a margin above the FP32 error bound; the
+//   others -- everything at or beyond yield -- run the FP64 return map
+//   (FP64 eigen-solve), so plastic flow is never computed in FP32;
+// * the shear strain rates, the spin and the heat stencil: sums of products
+//   of shape function derivatives with nodal values whose sum over the
+//   element vanishes, evaluated in FP32 on FP64 differences (v_i - v_0,
+//   T_j - T_i); the Jaumann rotation increments.  The normal strain rates
+//   stay FP64 (see k_strain_rate_mixed3).
 // The elastic and Maxwell increments stay FP64: the quasi-static explicit
 // scheme integrates their rounding without dissipating it (damping option 2
 // only scales the force), and in FP32 they alone moved the stress by 4e-6
@@ -139,52 +140,61 @@ __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *e
     return ldexp((double)expf(rr), (int)k);
 }
 
-// Mohr-Coulomb return map (rheology.cxx:151-299) on the FP64 trial stress s
-// (already holding the elastic trial), FP32 eigen-solve of its deviator.
-__device__ __forceinline__ unsigned elasto_plastic_mixed(double bulkm, double shearm, double amc, double anphi,
-                                                         double anpsi, double hardn, double ten_max,
-                                                         double &depls, double *s)
+// Screen of the Mohr-Coulomb yield test (rheology.cxx:163-178) in FP32.
+// The deviatoric trial stress D is diagonalised in FP32 (eigenvalues only);
+// the principal stresses and yield functions are formed in FP64 from the
+// FP64 mean stress.  Each computed eigenvalue lies within ||E||_2 of the
+// exact one (Weyl), E being the backward error of rounding D to FP32 and of
+// twelve Jacobi rotations: a few tens of eps32 ||D||_F.  The screen passes
+// an element only when both yield functions clear the surface by the margin
+// tol = 2^-12 ||D||_F (~4000 eps32 ||D||_F); every other element takes the
+// FP64 return map, so whatever yields follows the FP64 path exactly --
+// including the choice of principal directions when two principal stresses
+// (nearly) coincide, which FP32 cannot resolve and which decides the
+// direction of the plastic correction.
+__device__ __forceinline__ bool clearly_elastic_mixed(double amc, double anphi, double ten_max, const double *s)
 {
-    depls = 0;
     const double m = (s[0] + s[1] + s[2]) * (1.0 / 3);
-    float d[6] = {(float)(s[0] - m), (float)(s[1] - m), (float)(s[2] - m), (float)s[3], (float)s[4], (float)s[5]};
+    const float d[6] = {(float)(s[0] - m), (float)(s[1] - m), (float)(s[2] - m),
+                        (float)s[3], (float)s[4], (float)s[5]};
     float w[3], v[3][3];
     jacobi3f(d, w, v);
-    double p0 = m + (double)w[0], p2 = m + (double)w[2];
-    double fs = p0 - p2 * anphi + amc;
-    double ft = p2 - ten_max;
-    if (fs > 0 && ft < 0) return 0;
-    double pa = sqrt(1 + anphi * anphi) + anphi;
-    double ps = ten_max * anphi - amc;
-    double h = p2 - ten_max + pa * (p0 - ps);
-    double a1 = bulkm + 4. / 3 * shearm;
-    double a2 = bulkm - 2. / 3 * shearm;
-    double alam;
-    float c[3];
-    if (h < 0) {
-        alam = fs / (a1 - a2 * anpsi + a1 * anphi * anpsi - a2 * anphi + 2 * sqrt(anphi) * hardn);
-        c[0] = (float)(a1 - a2 * anpsi);
-        c[1] = (float)(a2 - a2 * anpsi);
-        c[2] = (float)(a2 - a1 * anpsi);
-        depls = fabs(alam) * sqrt((7 + 4 * anpsi + 7 * anpsi * anpsi) / 18);
-    } else {
-        alam = ft / a1;
-        c[0] = (float)a2;
-        c[1] = (float)a2;
-        c[2] = (float)a1;
-        depls = fabs(alam) * sqrt(7. / 18);
-    }
-    // s -= alam * sum_k c_k v_k v_k^T
-    float M[6];
-    M[0] = c[0] * v[0][0] * v[0][0] + c[1] * v[0][1] * v[0][1] + c[2] * v[0][2] * v[0][2];
-    M[1] = c[0] * v[1][0] * v[1][0] + c[1] * v[1][1] * v[1][1] + c[2] * v[1][2] * v[1][2];
-    M[2] = c[0] * v[2][0] * v[2][0] + c[1] * v[2][1] * v[2][1] + c[2] * v[2][2] * v[2][2];
-    M[3] = c[0] * v[0][0] * v[1][0] + c[1] * v[0][1] * v[1][1] + c[2] * v[0][2] * v[1][2];
-    M[4] = c[0] * v[0][0] * v[2][0] + c[1] * v[0][1] * v[2][1] + c[2] * v[0][2] * v[2][2];
-    M[5] = c[0] * v[1][0] * v[2][0] + c[1] * v[1][1] * v[2][1] + c[2] * v[1][2] * v[2][2];
+    const float nf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
+                           + 2.0f * (d[3] * d[3] + d[4] * d[4] + d[5] * d[5]));
+    const double tol = (double)nf * (1.0 / 4096);
+    const double p0 = m + (double)w[0], p2 = m + (double)w[2];
+    const double fs = p0 - p2 * anphi + amc;
+    const double ft = p2 - ten_max;
+    return fs > (1 + anphi) * tol && ft < -tol;
+}
+
+// maxwell (rheology.cxx:118-134) with 1/viscosity and 1/(1+tmp) by
+// recip_newton instead of two FP64 divisions; f1, f2 then differ from the
+// FP64 step's by a few ulp.  The divisions by 3 are div3, bit-identical.
+__device__ __forceinline__ void maxwell_mixed(double bulkm, double shearm, double viscosity, double dt, double dv,
+                                              const double *de, double *s)
+{
+    const double tmp = 0.5 * dt * shearm * recip_newton(viscosity);
+    const double f1 = 1 - tmp;
+    const double f2 = recip_newton(1 + tmp);
+    const double dev = div3(de[0] + de[1] + de[2]);
+    const double s0 = div3(s[0] + s[1] + s[2]);
+    const double g2 = 2 * shearm;
 #pragma unroll
-    for (int i = 0; i < 6; ++i) s[i] -= alam * (double)M[i];
-    return 0;
+    for (int i = 0; i < 3; ++i) s[i] = ((s[i] - s0) * f1 + g2 * (de[i] - dev)) * f2 + s0 + bulkm * dv;
+#pragma unroll
+    for (int i = 3; i < 6; ++i) s[i] = (s[i] * f1 + g2 * de[i]) * f2;
+}
+
+// relative volume change, evaluated as the FP64 step does (rheology.cxx:569,600):
+// vol/vol_old rounds to within 1.1e-16 of 1 + dv, an absolute error that the
+// bulk modulus integrates into the pressure every step.  A more accurate
+// form (an exact difference times a reciprocal) rounds differently, and that
+// alone moved the stress by 1.5e-6 (relative L2) against the FP64 step after
+// 2000 steps, so the mixed step keeps the FP64 step's rounding here.
+__device__ __forceinline__ double dvol_mixed(const KP &p, int e)
+{
+    return p.vol[e] / p.vol_old[e] - 1;
 }
 
 // update_stress (rheology.cxx:510-646), 3D, mixed precision
@@ -215,7 +225,7 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
     const double old_s = s[0] + s[1] + s[2];
     {
         const double div = edot[0] + edot[1] + edot[2];
-        const double corr = (edv - div) * (1.0 / 3);
+        const double corr = div3(edv - div);   // as the FP64 step rounds it
 #pragma unroll
         for (int i = 0; i < 3; ++i) edot[i] += corr;
     }
@@ -234,8 +244,7 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
     } else if (rt == DES_RH_VISCOUS) {
         viscous_<3>(bulkm, visc_mixed(p, e, edot, T), es[0] + es[1] + es[2], edot, s);
     } else if (rt == DES_RH_MAXWELL) {
-        const double dv = p.vol[e] / p.vol_old[e] - 1;
-        maxwell_<3>(bulkm, shearm, visc_mixed(p, e, edot, T), dt, dv, de, s);
+        maxwell_mixed(bulkm, shearm, visc_mixed(p, e, edot, T), dt, dvol_mixed(p, e), de, s);
     } else {
         double amc, anphi, anpsi, hardn, ten_max;
         m_plastic_props(p, e, pls, amc, anphi, anpsi, hardn, ten_max);
@@ -244,18 +253,23 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
         for (int i = 0; i < 6; ++i) sp[i] = s[i];
         elastic_<3>(bulkm, shearm, de, sp);
         double depls = 0;
-        bits |= elasto_plastic_mixed(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp);
+        if (!clearly_elastic_mixed(amc, anphi, ten_max, sp) &&
+            mc_return_<3>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp))
+            bits |= DES_DEV_QL_NOCONV;
         if (rt == DES_RH_EP) {
 #pragma unroll
             for (int i = 0; i < 6; ++i) s[i] = sp[i];
             pls += depls;
             dpls = depls;
         } else {   // EVP: the smaller second invariant wins (rheology.cxx:594-634)
-            const double dv = p.vol[e] / p.vol_old[e] - 1;
             double sv[6];
 #pragma unroll
             for (int i = 0; i < 6; ++i) sv[i] = s[i];
-            maxwell_<3>(bulkm, shearm, visc_mixed(p, e, edot, T), dt, dv, de, sv);
+            maxwell_mixed(bulkm, shearm, visc_mixed(p, e, edot, T), dt, dvol_mixed(p, e), de, sv);
+            // the choice is rounding-decided in near-lithostatic elements of high
+            // viscosity (J2 of a small deviator formed from pressure-sized
+            // components), and the two candidates differ in pressure (K dv
+            // against K tr(de)): J2 is evaluated exactly as the FP64 step does
             const double svII = second_invariant2_<3>(sv), spII = second_invariant2_<3>(sp);
             if (svII < spII) {
 #pragma unroll
@@ -281,7 +295,54 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
     if (bits) set_err(p, bits);
 }
 
-// strain rate (fields.cxx:166-232) from FP64 velocity differences, FP32 sums
+// strain rate (fields.cxx:166-232) from FP64 velocity differences.  Each
+// product dv_i,k * dN_i/dx_l is of the size of the whole row k of the
+// velocity gradient, so an FP32 sum carries an absolute error ~eps32 |L|
+// into every component.  In the shear components that is harmless, but the
+// normal components set the volumetric rate, which the pressure integrates
+// with the bulk modulus (through the nodal-mixed dvoldt): in FP32 they alone
+// moved the stress by 1e-4 (relative L2) in 150 steps of a yielding case.
+// So the normal components are FP64 (FP64 shape functions), the shear ones
+// FP32.
+__device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, double *out)
+{
+    const size_t ne = p.ne;
+    double v0[3];
+    load_node_v<3>(p, conn_at(p, 0, e), v0);
+    double dd[3][3];
+    float dv[3][3], sx[3], sy[3], sz[3];
+#pragma unroll
+    for (int i = 1; i < 4; ++i) {
+        double vi[3];
+        load_node_v<3>(p, conn_at(p, i, e), vi);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            dd[i - 1][d] = vi[d] - v0[d];
+            dv[i - 1][d] = (float)dd[i - 1][d];
+        }
+        sx[i - 1] = shp32_at(p, 0, i, e);
+        sy[i - 1] = shp32_at(p, 1, i, e);
+        sz[i - 1] = shp32_at(p, 2, i, e);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double *h = p.shp + (size_t)k * 4 * ne + e;   // dN_i/dx_k at h[i * ne]
+        out[k] = dd[0][k] * h[ne] + dd[1][k] * h[2 * ne] + dd[2][k] * h[3 * ne];
+    }
+    float s3 = 0, s4 = 0, s5 = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        s3 += 0.5f * (dv[i][0] * sy[i] + dv[i][1] * sx[i]);
+        s4 += 0.5f * (dv[i][0] * sz[i] + dv[i][2] * sx[i]);
+        s5 += 0.5f * (dv[i][1] * sz[i] + dv[i][2] * sy[i]);
+    }
+    out[3] = (double)s3;
+    out[4] = (double)s4;
+    out[5] = (double)s5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) p.srate[c * ne + e] = out[c];
+}
+
 __global__ void __launch_bounds__(TPB_M) k_strain_rate_mixed3(KP p, int begin_step)
 {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -290,31 +351,8 @@ __global__ void __launch_bounds__(TPB_M) k_strain_rate_mixed3(KP p, int begin_st
         p.clk->time += p.clk->dt;
     }
     if (e >= p.ne) return;
-    double v0[3];
-    load_node_v<3>(p, conn_at(p, 0, e), v0);
-    float dv[3][3], sx[3], sy[3], sz[3];
-#pragma unroll
-    for (int i = 1; i < 4; ++i) {
-        double vi[3];
-        load_node_v<3>(p, conn_at(p, i, e), vi);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) dv[i - 1][d] = (float)(vi[d] - v0[d]);
-        sx[i - 1] = shp32_at(p, 0, i, e);
-        sy[i - 1] = shp32_at(p, 1, i, e);
-        sz[i - 1] = shp32_at(p, 2, i, e);
-    }
-    float s[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        s[0] += dv[i][0] * sx[i];
-        s[1] += dv[i][1] * sy[i];
-        s[2] += dv[i][2] * sz[i];
-        s[3] += 0.5f * (dv[i][0] * sy[i] + dv[i][1] * sx[i]);
-        s[4] += 0.5f * (dv[i][0] * sz[i] + dv[i][2] * sx[i]);
-        s[5] += 0.5f * (dv[i][1] * sz[i] + dv[i][2] * sy[i]);
-    }
-#pragma unroll
-    for (int c = 0; c < 6; ++c) p.srate[(size_t)c * p.ne + e] = (double)s[c];
+    double sr[6];
+    strain_rate_mixed_elem(p, e, sr);
 }
 
 // heat stencil on FP64 temperature differences (sum_j D_ij = 0), FP32
@@ -354,6 +392,88 @@ __global__ void __launch_bounds__(TPB_M) k_heat_dvoldt_mixed3(KP p, int heat, in
     if (do_dvoldt) p.ntmp[n] = dvoldt / p.vol_n[n];
 }
 
+// ------------------------------------------------------------------
+// Fused step: strain rate, heat, dvoldt and the temperature update as one
+// element pass and one node pass.  The per-pair work of the node-centric
+// gather above (k_heat_dvoldt_mixed3: the stencil row of the node's slot,
+// four temperature differences and their FP32 conversions, which issue on
+// the FP64 pipe) is done once per element: the element pass stores the
+// four FP32 heat terms of the element and its dvoldt term, and the node
+// pass sums them over the support list in ascending element order.  Each
+// term is the very value the gather forms for that (node, element) pair,
+// and the sums run in the same order, so the result is bit-identical to
+// k_strain_rate_mixed3 + k_heat_dvoldt_mixed3 + k_temperature_update.
+// ------------------------------------------------------------------
+__global__ void __launch_bounds__(TPB_M) k_elem_pass_mixed3(KP p, int heat)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e == 0) {   // var.steps++; var.time += var.dt (dynearthsol.cxx:325-326)
+        p.clk->steps += 1;
+        p.clk->time += p.clk->dt;
+    }
+    if (e >= p.ne) return;
+    const size_t ne = p.ne;
+    double sr[6];
+    strain_rate_mixed_elem(p, e, sr);
+    const double vol = p.vol[e];
+    p.qv[e] = (sr[0] + sr[1] + sr[2]) * vol;   // compute_dvoldt term (geometry.cxx:127-135)
+    if (!heat) return;
+    double T[4];
+    float sx[4], sy[4], sz[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        T[i] = p.T[conn_at(p, i, e)];
+        sx[i] = shp32_at(p, 0, i, e);
+        sy[i] = shp32_at(p, 1, i, e);
+        sz[i] = shp32_at(p, 2, i, e);
+    }
+    // D_ij = D_ji and (float)(T_i - T_j) = -(float)(T_j - T_i) bit for bit,
+    // so each of the six products serves both rows
+    float P[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = i + 1; j < 4; ++j) {
+            const float D = sx[i] * sx[j] + sy[i] * sy[j] + sz[i] * sz[j];
+            const float t = D * (float)(T[j] - T[i]);
+            P[i][j] = t;
+            P[j][i] = -t;
+        }
+    const bool k_const = (p.mat.nmat == 1) && !p.ef[DES_EF_THERM_COND];
+    const float volf = (float)vol;
+    const float kv = (float)(k_const ? p.mat.therm_cond[0] : m_k(p, e)) * volf;
+    const float rh = (float)((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * volf;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float diffusion = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j != i) diffusion += P[i][j];
+        p.hc[(size_t)i * ne + e] = kv * diffusion - rh;
+    }
+}
+
+__global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat)
+{
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.nn) return;
+    const size_t ne = p.ne;
+    double tdot = 0, dvoldt = 0;
+    for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+        const int ent = p.sup_ent[q];
+        const int e = ent >> 2, i = ent & 3;
+        if (heat) tdot += (double)p.hc[(size_t)i * ne + e];
+        dvoldt += p.qv[e];
+    }
+    p.ntmp[n] = dvoldt / p.vol_n[n];
+    if (heat) {   // temperature update + Dirichlet BC (fields.cxx:151-162)
+        const unsigned flag = p.bcflag[n];
+        if (flag & BOUNDZ1) p.T[n] = p.prm.surface_temperature;
+        else if ((flag & BOUNDZ0) && !p.prm.has_fixed_bottom_temperature) p.T[n] = p.prm.mantle_temperature;
+        else p.T[n] -= tdot * p.clk->dt / p.tmass[n];
+    }
+}
+
 int launch_update_stress_mixed(const KP &p, cudaStream_t s, bool fused)
 {
     k_update_stress_mixed3<<<nblocks_m(p.ne), TPB_M, 0, s>>>(p, (int)fused);
@@ -373,5 +493,17 @@ int launch_heat_and_dvoldt_mixed(const KP &p, cudaStream_t s, bool heat, bool dv
 }
 
 
+
+int launch_elem_pass_mixed(const KP &p, cudaStream_t s, bool heat)
+{
+    k_elem_pass_mixed3<<<nblocks_m(p.ne), TPB_M, 0, s>>>(p, (int)heat);
+    return 1;
+}
+
+int launch_node_pass_mixed(const KP &p, cudaStream_t s, bool heat)
+{
+    k_node_pass_mixed3<<<nblocks_m(p.nn), TPB_M, 0, s>>>(p, (int)heat);
+    return 1;
+}
 
 }  // namespace des

@@ -10,5 +10,8 @@ namespace des {
 int launch_update_stress_mixed(const KP &p, cudaStream_t s, bool fused);
 int launch_strain_rate_mixed(const KP &p, cudaStream_t s, bool begin_step);
 int launch_heat_and_dvoldt_mixed(const KP &p, cudaStream_t s, bool heat, bool dvoldt);
+// fused step: strain rate + heat terms + dvoldt terms, then the nodal sums and the temperature update
+int launch_elem_pass_mixed(const KP &p, cudaStream_t s, bool heat);
+int launch_node_pass_mixed(const KP &p, cudaStream_t s, bool heat);
 
 }  // namespace des

@@ -253,8 +253,8 @@ __device__ __forceinline__ void maxwell_(double bulkm, double shearm, double vis
     double tmp = 0.5 * dt * shearm / viscosity;
     double f1 = 1 - tmp;
     double f2 = 1 / (1 + tmp);
-    double dev = trace_<ND>(de) / ND;
-    double s0 = trace_<ND>(s) / ND;
+    double dev = divnd<ND>(trace_<ND>(de));
+    double s0 = divnd<ND>(trace_<ND>(s));
 #pragma unroll
     for (int i = 0; i < ND; ++i) s[i] = ((s[i] - s0) * f1 + 2 * shearm * (de[i] - dev)) * f2 + s0 + bulkm * dv;
 #pragma unroll
@@ -267,19 +267,20 @@ __device__ __forceinline__ void viscous_(double bulkm, double viscosity, double 
                                          double *s)
 {
     constexpr int NSTR = ND * (ND + 1) / 2;
-    double dev = trace_<ND>(edot) / ND;
+    double dev = divnd<ND>(trace_<ND>(edot));
 #pragma unroll
     for (int i = 0; i < ND; ++i) s[i] = 2 * viscosity * (edot[i] - dev) + bulkm * total_dv;
 #pragma unroll
     for (int i = ND; i < NSTR; ++i) s[i] = 2 * viscosity * edot[i];
 }
 
-// elasto_plastic: Mohr-Coulomb return map in principal space (rheology.cxx:151-299)
+// Mohr-Coulomb return map in principal space of the elastic trial stress s
+// (rheology.cxx:163-299).  Returns nonzero when the QL fallback of the
+// eigen-solver hit its sweep cap.
 template <int ND>
-__device__ int elasto_plastic_(double bulkm, double shearm, double amc, double anphi, double anpsi,
-                               double hardn, double ten_max, const double *de, double &depls, double *s)
+__device__ int mc_return_(double bulkm, double shearm, double amc, double anphi, double anpsi, double hardn,
+                          double ten_max, double &depls, double *s)
 {
-    elastic_<ND>(bulkm, shearm, de, s);
     depls = 0;
     double p[3];
     double v[3][3];
@@ -335,6 +336,15 @@ __device__ int elasto_plastic_(double bulkm, double shearm, double amc, double a
         s[2] = 0.5 * (p[0] - p[1]) * sin2t;
     }
     return rc;
+}
+
+// elasto_plastic (rheology.cxx:151-299): elastic trial stress, then the return map
+template <int ND>
+__device__ int elasto_plastic_(double bulkm, double shearm, double amc, double anphi, double anpsi,
+                               double hardn, double ten_max, const double *de, double &depls, double *s)
+{
+    elastic_<ND>(bulkm, shearm, de, s);
+    return mc_return_<ND>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, s);
 }
 
 // elasto_plastic2d: plane-strain Mohr-Coulomb (rheology.cxx:302-507)
@@ -433,7 +443,7 @@ __device__ unsigned update_stress_elem(const KP &p, int e, double dt, double *s,
     {
         double div = trace_<ND>(edot);
 #pragma unroll
-        for (int i = 0; i < ND; ++i) edot[i] += (edvoldt - div) / ND;
+        for (int i = 0; i < ND; ++i) edot[i] += divnd<ND>(edvoldt - div);
     }
 #pragma unroll
     for (int i = 0; i < NSTR; ++i) es[i] += edot[i] * dt;

@@ -4,10 +4,13 @@ The gate of the mixed step is a relative L2 stress error of at most 1e-6
 against the FP64 run from the same state (||s_mixed - s_fp64||_2 /
 ||s_fp64||_2 over all elements and components); the normalised maximum
 error of every other field is reported.  Over long horizons with the
-default damping (option 1) the reference's own FP64 step is chaotic (a
-one-ulp libm change moves the stress by ~1e-4 after ~1000 steps), so the
-long-horizon gate uses the continuous damping option 2, and the default
-damping is gated over a 250-step horizon before that divergence sets in.
+default damping (option 1) the reference's own FP64 step is chaotic: its
+copysign on the nodal velocity turns any rounding difference at a node
+whose velocity changes sign into an O(1) change of that node's damping
+force, so that a one-ulp libm change moves the stress by ~1e-4 after ~1000
+steps.  The long-horizon gate therefore uses the continuous damping option 2
+(2000 steps), and the default damping is gated over 50 steps, before that
+divergence sets in.
 """
 import numpy as np
 import pytest
@@ -39,18 +42,20 @@ def _pair(wl, nsteps):
 
 
 def test_gpu_mixed_stress_error_default_damping_short_horizon():
-    """Default damping (option 1): gated over 10 steps.  Past that the
-    damping's copysign turns the mixed step's rounding into O(1) velocity
-    differences at nodes whose velocity changes sign, so the longer-horizon
-    errors are printed, not gated."""
+    """Default damping (option 1): gated over 10 and 50 steps.  The
+    250-step error is printed, not gated: by then the damping's copysign
+    has amplified the rounding differences (as it does between two FP64
+    builds that differ by one ulp in a libm function)."""
     from dynearthsol_gb300.config import make_workload
     wl = make_workload("c1_3d_evp", cells=(20, 20, 6))
     l2, errs, a, b = _pair(wl, 10)
     print("mixed vs fp64, default damping, 10 steps: L2 stress", l2, errs)
-    for n in (50, 250):
-        l2n, _, _, _ = _pair(wl, n)
-        print(f"  ... after {n} steps: L2 stress {l2n:.3e}")
+    l2_50, errs_50, _, _ = _pair(wl, 50)
+    print(f"  ... after 50 steps: L2 stress {l2_50:.3e}")
+    l2_250, _, _, _ = _pair(wl, 250)
+    print(f"  ... after 250 steps: L2 stress {l2_250:.3e}")
     assert l2 <= 1e-6, (l2, errs)
+    assert l2_50 <= 1e-6, (l2_50, errs_50)
 
 
 def test_gpu_mixed_stress_error_damping2_2000_steps():
@@ -67,8 +72,9 @@ def test_gpu_mixed_stress_error_damping2_2000_steps():
 
 def test_gpu_mixed_yielding_damping2_vs_fp64():
     """The fast-yielding case (Mohr-Coulomb return map active in most
-    elements, where the FP32 eigen-solve enters) with damping option 2:
-    mixed vs FP64 over the case's 150 steps."""
+    elements: there the FP32 yield screen hands the element to the FP64
+    return map) with damping option 2: mixed vs FP64 over the case's 150
+    steps."""
     from dataclasses import replace
     from cases import build_case
     wl, n = build_case("3d_evp_yield")
