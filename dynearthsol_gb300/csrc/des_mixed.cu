@@ -186,12 +186,7 @@ __device__ __forceinline__ void maxwell_mixed(double bulkm, double shearm, doubl
     for (int i = 3; i < 6; ++i) s[i] = (s[i] * f1 + g2 * de[i]) * f2;
 }
 
-// relative volume change, evaluated as the FP64 step does (rheology.cxx:569,600):
-// vol/vol_old rounds to within 1.1e-16 of 1 + dv, an absolute error that the
-// bulk modulus integrates into the pressure every step.  A more accurate
-// form (an exact difference times a reciprocal) rounds differently, and that
-// alone moved the stress by 1.5e-6 (relative L2) against the FP64 step after
-// 2000 steps, so the mixed step keeps the FP64 step's rounding here.
+// relative volume change, evaluated as the FP64 step does (rheology.cxx:569,600)
 __device__ __forceinline__ double dvol_mixed(const KP &p, int e)
 {
     return p.vol[e] / p.vol_old[e] - 1;
