@@ -292,6 +292,11 @@ def main():
     ap.add_argument("--no-compare", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--gate-steps", type=int, default=2000,
                     help="steps of the damping-2 mixed-vs-FP64 stress-error gate (0: skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=500,
+                    help="window of the adjoint benchmark (0: skip it)")
+    ap.add_argument("--adjoint-every", type=int, default=50, help="checkpoint spacing of the adjoint window")
+    ap.add_argument("--adjoint-fd", type=int, default=4,
+                    help="elements checked against central differences in the adjoint benchmark")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -366,6 +371,9 @@ def main():
     e2e = None
     if args.e2e_steps > 0:
         e2e = run_e2e(args, m, wl, init, clock0, world, dist)
+    adjoint = None
+    if args.adjoint_steps > 0 and rank == 0:
+        adjoint = adjoint_bench(args, stream)
     if rank == 0:
         line = {
             "metric": metric_name(args), "value": value, "unit": "Mtet-steps/s", "n_gpus": world,
@@ -380,6 +388,7 @@ def main():
             "mixed_vs_fp64": compare,
             "mixed_error_gate": gate,
             "e2e": e2e,
+            "adjoint": adjoint,
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
@@ -392,6 +401,97 @@ def main():
     m.close()
     f64.close()
     return 0
+
+
+def adjoint_bench(args, stream):
+    """Adjoint/forward wall-time ratio on the 998,400-tet adjoint case: a
+    window of K FP64 steps (dt held) with a checkpoint every C steps; loss =
+    the top-surface velocity misfit against a target run whose log10
+    viscosity field is a seeded Gaussian random field (mean 21, sd 0.5,
+    correlation length 15 km), evaluated at another draw of the field.  The
+    log10-viscosity gradient is checked by fourth-order central differences
+    (steps of 0.01) at
+    `adjoint_fd` elements drawn among those whose gradient is at least 1% of
+    the largest; below that step the differences of the quasi-static
+    velocity misfit are dominated by rounding (~3e-11 of the loss, which a
+    single element's share of the gradient barely exceeds over 500 steps).
+    The directional derivative along the normalised gradient (unit step in
+    log10 viscosity, ~1e-3 per element) carries the whole gradient's signal."""
+    import torch
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.adjoint import Window, adjoint_workload, fd5, surface_velocity_misfit, top_nodes
+    from dynearthsol_gb300.config import initial_state
+    from dynearthsol_gb300.solver import DeviceModel
+    K, C = args.adjoint_steps, args.adjoint_every
+    wl, lv_t, lv_s = adjoint_workload()
+    st, cp = initial_state(wl)
+    m = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_FP64, stream=stream.cuda_stream)
+    init = m.init_fields(st)
+    clock0 = m.clock()
+    win = Window(m, init, clock0, K, C)
+    nodes = top_nodes(wl.mesh)
+    LV = capi.EF_LOG10_VISC
+    target = win.run({LV: lv_t})["vel"]
+
+    def loss_of(lv):
+        return surface_velocity_misfit(win.run({LV: lv})["vel"], target, nodes)[0]
+
+    # timed forward (recording checkpoints) and reverse sweep
+    win.set_params({LV: lv_s})
+    m.upload(win.start, clock0)
+    m.sync()
+    t0 = time.perf_counter()
+    m.adjoint_forward(K, C)
+    m.sync()
+    t_fwd = time.perf_counter() - t0
+    fin = m.download()
+    loss, seed = surface_velocity_misfit(fin["vel"], target, nodes)
+    yielded = int((fin["plstrain"] > init["plstrain"] + 1e-12).sum())
+    m.sync()
+    t0 = time.perf_counter()
+    _, grad = m.adjoint_backward({"vel": seed}, want_start=False)
+    m.sync()
+    t_bwd = time.perf_counter() - t0
+    # the plain (graph-replayed) step over the same window, for reference
+    m.upload(win.start, clock0)
+    m.sync()
+    t0 = time.perf_counter()
+    m.step(K)
+    m.sync()
+    t_step = time.perf_counter() - t0
+    g = grad[LV]
+    rng = np.random.default_rng(2024)
+    cand = np.nonzero(np.abs(g) >= 0.01 * np.abs(g).max())[0]
+    fd = []
+    for e in rng.choice(cand, size=min(args.adjoint_fd, len(cand)), replace=False):
+        def along(t, e=e):
+            lv = lv_s.copy()
+            lv[e] += t
+            return loss_of(lv)
+        d = fd5(along, 1e-2)
+        fd.append({"elem": int(e), "adjoint": float(g[e]), "central_fd": float(d),
+                   "rel_err": float(abs(d - g[e]) / max(abs(d), abs(g[e]), 1e-300))})
+    # directional derivative along the normalised gradient: the whole
+    # gradient's signal, well above the rounding of the misfit
+    gn = np.linalg.norm(g)
+    ghat = g / gn
+
+    def along_g(t):
+        return loss_of(lv_s + t * ghat)
+
+    dfd = fd5(along_g, 1.0)
+    gdir = {"step": 1.0, "adjoint": float(gn), "central_fd": float(dfd),
+            "rel_err": float(abs(dfd - gn) / max(abs(dfd), gn))}
+    m.close()
+    return {"workload": "c3_3d_adjoint", "nelem": wl.mesh.nelem, "window_steps": K, "checkpoint_every": C,
+            "loss": loss, "yielded_elements": yielded, "forward_s": t_fwd, "adjoint_s": t_bwd, "adjoint_over_forward": t_bwd / t_fwd,
+            "graph_step_s": t_step, "adjoint_over_graph_step": t_bwd / t_step,
+            "gradients": "log10 viscosity, shear modulus, cohesion0/1, friction0/1 per element; vbc_values",
+            "vbc_grad_x": [float(grad["vbc_values"][0]), float(grad["vbc_values"][1])],
+            "fd_check": fd, "fd_max_rel_err": max((r["rel_err"] for r in fd), default=None),
+            "fd_gradient_direction": gdir,
+            "dt": "held at the start value (compute_dt not called in the window)",
+            "damping_option": 2}
 
 
 def run_e2e(args, m, wl, init, clock0, world, dist):

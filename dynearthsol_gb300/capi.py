@@ -137,6 +137,12 @@ class DesHostState(C.Structure):
     ]
 
 
+class DesAdjointGrad(C.Structure):
+    """des_adjoint_grad: per-element gradient arrays (NULL = skip) and the
+    gradient with respect to each boundary's prescribed velocity value."""
+    _fields_ = [("elem", _dp * EF_COUNT), ("vbc_values", C.c_double * NBDRY)]
+
+
 def dptr(a: np.ndarray | None):
     """double* of a C-contiguous float64 array (NULL for None)."""
     if a is None:
@@ -206,6 +212,9 @@ _SIGS = {
     "des_synchronize": [C.c_void_p],
     "des_launch_count": [C.c_void_p, C.POINTER(C.c_longlong)],
     "des_nmd_stress_noalloc": [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 8,
+    "des_adjoint_forward": [C.c_void_p, C.c_int, C.c_int],
+    "des_adjoint_backward": [C.c_void_p, C.POINTER(DesHostState), C.POINTER(DesHostState),
+                             C.POINTER(DesAdjointGrad)],
 }
 
 

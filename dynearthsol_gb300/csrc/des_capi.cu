@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 
+#include "des_ctx.cuh"
 #include "des_kernels.cuh"
 #include "des_mixed.cuh"
 
@@ -33,28 +34,6 @@ int fail_msg(std::string &dst, int code, const char *fmt, ...)
 }
 
 }  // namespace
-
-struct des_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int precision = DES_PREC_FP64;
-    int nd = 0, npe = 0, nstr = 0, nn = 0, ne = 0, nbf = 0;
-    KP kp{};                      // per-function parameter block (no step scratch)
-    char *pool = nullptr;         // one device allocation for every array
-    size_t pool_bytes = 0;
-    double *d_tdot = nullptr;     // node scratch of the fused step
-    double *d_rho = nullptr;      // element scratch of the fused step
-    double *d_stage = nullptr;    // AoS staging buffer
-    size_t stage_doubles = 0;
-    unsigned long long *d_red = nullptr;
-    double *d_ef[DES_EF_COUNT] = {};
-    cudaGraphExec_t step_exec = nullptr;
-    int step_kernels = 0;
-    long long launches = 0;
-    std::string err;
-    bool has_state = false;
-};
 
 namespace {
 
@@ -460,6 +439,7 @@ int des_destroy(des_ctx *c)
     if (!c) return DES_OK;
     cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
+    adj_free(c);
     for (int k = 0; k < DES_EF_COUNT; ++k)
         if (c->d_ef[k]) cudaFree(c->d_ef[k]);
     cudaFree(c->pool);
@@ -987,3 +967,33 @@ int des_launch_count(des_ctx *c, long long *count)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------
+// helpers shared with the other translation units of the context
+// ------------------------------------------------------------------
+namespace des {
+
+int ctx_fail(des_ctx *c, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+    return code;
+}
+
+int ctx_cuda_fail(des_ctx *c, cudaError_t e, const char *what) { return cuda_fail(c, e, what); }
+int ctx_check_launch(des_ctx *c, int n) { return check_launch(c, n); }
+KP ctx_step_kp(const des_ctx *c) { return step_kp(c); }
+int ctx_put_field(des_ctx *c, const double *host, double *dev, int n, int ncomp)
+{
+    return put_field(c, host, dev, n, ncomp);
+}
+int ctx_get_field(des_ctx *c, const double *dev, double *host, int n, int ncomp)
+{
+    return get_field(c, host, dev, n, ncomp);
+}
+
+}  // namespace des

@@ -1,0 +1,51 @@
+// des_ctx.cuh -- the device context behind the C ABI (internal to the
+// library: des_capi.cu and the adjoint's host side share it).
+#pragma once
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/desgpu.h"
+#include "des_common.cuh"
+
+namespace des {
+struct AdjWork;
+}
+
+struct des_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int precision = DES_PREC_FP64;
+    int nd = 0, npe = 0, nstr = 0, nn = 0, ne = 0, nbf = 0;
+    des::KP kp{};                 // per-function parameter block (no step scratch)
+    char *pool = nullptr;         // one device allocation for every array
+    size_t pool_bytes = 0;
+    double *d_tdot = nullptr;     // node scratch of the fused step
+    double *d_rho = nullptr;      // element scratch of the fused step
+    double *d_stage = nullptr;    // AoS staging buffer
+    size_t stage_doubles = 0;
+    unsigned long long *d_red = nullptr;
+    double *d_ef[DES_EF_COUNT] = {};
+    cudaGraphExec_t step_exec = nullptr;
+    int step_kernels = 0;
+    long long launches = 0;
+    std::string err;
+    bool has_state = false;
+    des::AdjWork *adj = nullptr;  // reverse-mode workspace, created on first use
+};
+
+namespace des {
+
+// helpers of des_capi.cu for the other translation units of the context
+int ctx_fail(des_ctx *c, int code, const char *fmt, ...);
+int ctx_cuda_fail(des_ctx *c, cudaError_t e, const char *what);
+int ctx_check_launch(des_ctx *c, int n);
+KP ctx_step_kp(const des_ctx *c);
+// state transfer between host AoS rows and device SoA arrays (staging buffer)
+int ctx_put_field(des_ctx *c, const double *host, double *dev, int n, int ncomp);
+int ctx_get_field(des_ctx *c, const double *dev, double *host, int n, int ncomp);
+// frees the reverse-mode workspace (des_adjoint_host.cu)
+void adj_free(des_ctx *c);
+
+}  // namespace des

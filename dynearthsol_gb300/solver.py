@@ -149,3 +149,53 @@ class DeviceModel:
         n = C.c_longlong()
         self._check(self.lib.des_launch_count(self.ctx, C.byref(n)))
         return n.value
+
+    # -- parameters --
+    def set_elem_field(self, field: int, values: np.ndarray):
+        """Per-element override (capi.EF_*) of a material property."""
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        self._ef[field] = a
+        self._check(self.lib.des_set_elem_field(self.ctx, field, capi.dptr(a)))
+
+    def set_params(self, **changes):
+        """Change run-time parameters (des_params fields) of the context."""
+        for k, v in changes.items():
+            if k == "vbc_values":
+                for i, x in enumerate(v):
+                    self.cs.params.vbc_values[i] = float(x)
+            else:
+                setattr(self.cs.params, k, v)
+        self._check(self.lib.des_set_params(self.ctx, C.byref(self.cs.params)))
+
+    # -- reverse mode --
+    ADJOINT_FIELDS = ("coord", "vel", "temperature", "stress", "plstrain")
+
+    def adjoint_forward(self, nsteps: int, checkpoint_every: int):
+        """Run a window of nsteps steps (dt held) recording checkpoints."""
+        self._check(self.lib.des_adjoint_forward(self.ctx, nsteps, checkpoint_every))
+
+    def adjoint_backward(self, seed: dict, want_start: bool = True):
+        """Reverse sweep of the recorded window.  seed: adjoints of the final
+        state (any of ADJOINT_FIELDS, reference layout).  Returns (start, grad):
+        the adjoints of the window's start state and a dict with one [nelem]
+        gradient per capi.EF_* field and 'vbc_values' [10]."""
+        m = self.wl.mesh
+        nd, nn, ne = m.ndims, m.nnode, m.nelem
+        shapes = {"coord": (nn, nd), "vel": (nn, nd), "temperature": (nn,), "stress": (ne, nstr_of(nd)),
+                  "plstrain": (ne,)}
+        sd = {k: np.ascontiguousarray(seed[k], dtype=np.float64) for k in self.ADJOINT_FIELDS if k in seed}
+        for k, a in sd.items():
+            if a.shape != shapes[k]:
+                raise ValueError(f"seed {k}: shape {a.shape}, expected {shapes[k]}")
+        hs_seed = capi.host_state_struct(sd)
+        start = {k: np.zeros(shapes[k]) for k in self.ADJOINT_FIELDS} if want_start else {}
+        hs_start = capi.host_state_struct(start)
+        g = capi.DesAdjointGrad()
+        garr = [np.zeros(ne) for _ in range(capi.EF_COUNT)]
+        for k in range(capi.EF_COUNT):
+            g.elem[k] = capi.dptr(garr[k])
+        self._check(self.lib.des_adjoint_backward(self.ctx, C.byref(hs_seed),
+                                                  C.byref(hs_start) if want_start else None, C.byref(g)))
+        grad = {k: garr[k] for k in range(capi.EF_COUNT)}
+        grad["vbc_values"] = np.array(list(g.vbc_values))
+        return start, grad

@@ -275,6 +275,38 @@ int des_step(des_ctx *ctx, int nsteps);
  * This is the drop-in form for a caller whose Variables stay authoritative. */
 int des_step_host(des_ctx *ctx, des_host_state *st, int nsteps);
 
+/* ---- reverse mode: the adjoint of a window of steps --------------------
+ * No counterpart in the reference.  Gradients of a scalar loss of the
+ * state after a window of nsteps steps of the 3D FP64 step, taken with dt
+ * held at the context's dt over the window (compute_dt is not called
+ * inside it; des_step with fixed_dt = that dt takes the same steps).
+ * Supported: 3D, DES_PREC_FP64, one material without element markers,
+ * rheology elastic, Maxwell, elasto-plastic or elasto-visco-plastic.  Kinks
+ * (yield, the EVP branch choice, viscosity clamps, damping signs, BC
+ * overwrites) take the derivative of the branch the forward took.
+ *
+ * des_adjoint_forward runs the window from the current state, keeping the
+ * state every checkpoint_every steps, and leaves the context at the
+ * window's end.  des_adjoint_backward takes the adjoint of that final state
+ * in seed (its fields coord, vel, temperature, stress and plstrain, in
+ * des_host_state's layout; NULL fields are zero), recomputes each segment
+ * from its checkpoint and runs the reverse steps.  It writes the adjoint
+ * of the window's start state to the same five fields of start_adjoint
+ * (NULL fields, or start_adjoint NULL, are skipped) and the gradients to
+ * grad, and leaves the context at the window's end.  It may be called
+ * again with another seed until the next des_adjoint_forward. */
+typedef struct des_adjoint_grad {
+    /* [nelem] d loss / d (the element's value of DES_EF_k), or NULL.
+     * DES_EF_LOG10_VISC only when that field is set (it replaces the
+     * viscosity law); the others whether or not the field is set. */
+    double *elem[DES_EF_COUNT];
+    double vbc_values[DES_NBDRYTYPES];   /* d loss / d des_params.vbc_values[i] */
+} des_adjoint_grad;
+
+int des_adjoint_forward(des_ctx *ctx, int nsteps, int checkpoint_every);
+int des_adjoint_backward(des_ctx *ctx, const des_host_state *seed, des_host_state *start_adjoint,
+                         des_adjoint_grad *grad);
+
 /* ---- nodal-mixed pressure smoothing without any device allocation ---- */
 /* No counterpart in the reference: an extra entry point for callers that
  * cannot allocate device memory -- a host application that owns every

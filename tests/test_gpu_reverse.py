@@ -1,0 +1,271 @@
+"""Reverse mode (des_adjoint_forward / des_adjoint_backward) against central
+finite differences of the forward window, on small meshes.
+
+The loss is linear in the final state, L = <seed, S_K> over coordinates,
+velocities, temperature, stress and plastic strain, so its adjoint is the
+seed.  For a direction d in the start state or in the parameters, the
+adjoint's <adjoint, d> must equal (L(p + d) - L(p - d)) / 2.  Directions
+are scaled to ~1e-6 of each field, so the central difference is accurate
+to ~1e-9 where the step is smooth; the kinks of the forward (yield, the
+EVP choice, viscosity clamps) are stepped over only where they are not
+met within the perturbation.  Damping option 2 (continuous) is used: with
+option 1 the step is discontinuous in the velocity sign.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("coord", "vel", "temperature", "stress", "plstrain")
+
+
+def _window(wl, K, C, spin=4):
+    from dynearthsol_gb300.adjoint import Window
+    from dynearthsol_gb300.config import initial_state
+    from dynearthsol_gb300.solver import DeviceModel
+    st, cp = initial_state(wl)
+    m = DeviceModel(wl, comp_pressure=cp)
+    m.init_fields(st)
+    if spin:
+        m.step(spin)   # nonzero velocities and deviatoric stresses
+    return Window(m, m.download(), m.clock(), K, C)
+
+
+def _workload(name="c1_3d_evp", cells=(3, 3, 2), **params):
+    from dataclasses import replace
+    from dynearthsol_gb300.config import make_workload
+    wl = make_workload(name, cells=cells)
+    wl.params = replace(wl.params, damping_option=2, **params)
+    return wl
+
+
+def _seed(win, rng):
+    final = win.run()
+    seed = {}
+    for k in FIELDS:
+        a = final[k]
+        sc = max(float(np.abs(a).max()), 1e-30)
+        seed[k] = rng.standard_normal(a.shape) / sc
+    return seed
+
+
+def _dstate(win, rng, field, scale=1e-6):
+    s = win.start
+    a = s[field]
+    if field == "coord":
+        ext = s["coord"].max(axis=0) - s["coord"].min(axis=0)
+        d = rng.standard_normal(a.shape) * (ext / 10)
+    elif field == "plstrain":
+        d = np.where(a > 1e-3, rng.standard_normal(a.shape) * np.maximum(a, 1e-3), 0.0)
+    else:
+        d = rng.standard_normal(a.shape) * max(float(np.abs(a).max()), 1e-30)
+    return {field: d * scale}
+
+
+def _check(win, seed, dstate=None, dparams=None, params=None):
+    from dynearthsol_gb300.adjoint import adjoint_dot, central_fd
+    win.run(params)
+    start, grad = win.gradients(seed)
+    ad = adjoint_dot(start, grad, dstate, dparams)
+    fd = central_fd(win, seed, dstate, dparams, params=params)
+    rel = abs(ad - fd) / max(abs(ad), abs(fd), 1e-300)
+    return ad, fd, rel
+
+
+def test_reverse_one_step_start_state():
+    """One step, each start-state field alone: adjoint vs central difference."""
+    rng = np.random.default_rng(1)
+    win = _window(_workload(), 1, 1)
+    seed = _seed(win, rng)
+    worst = 0.0
+    for f in ("coord", "vel", "temperature", "stress"):
+        ad, fd, rel = _check(win, seed, dstate=_dstate(win, rng, f))
+        print(f"  d{f:12s} adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+        worst = max(worst, rel)
+    assert worst <= 1e-6, worst
+
+
+def test_reverse_one_step_parameters():
+    """One step, each parameter alone: shear modulus, cohesion, friction
+    angle, conductivity and the prescribed boundary velocities.  The
+    conductivity moves only the temperature, by ~1e-12 of the loss: it is
+    checked on a temperature seed with a 1e-3 step."""
+    from dynearthsol_gb300 import capi
+    rng = np.random.default_rng(2)
+    wl = _workload()
+    ne = wl.mesh.nelem
+    wl.elem_fields = {capi.EF_SHEAR_MODULUS: np.full(ne, wl.mat.shear_modulus[0]),
+                      capi.EF_COHESION0: np.full(ne, wl.mat.cohesion0[0]),
+                      capi.EF_COHESION1: np.full(ne, wl.mat.cohesion1[0]),
+                      capi.EF_FRICTION0: np.full(ne, wl.mat.friction_angle0[0]),
+                      capi.EF_FRICTION1: np.full(ne, wl.mat.friction_angle1[0]),
+                      capi.EF_THERM_COND: np.full(ne, wl.mat.therm_cond[0])}
+    win = _window(wl, 1, 1)
+    seed = _seed(win, rng)
+    worst = 0.0
+    for k, base in wl.elem_fields.items():
+        if k == capi.EF_THERM_COND:
+            continue
+        d = rng.standard_normal(ne) * 1e-6 * np.abs(base)
+        ad, fd, rel = _check(win, seed, dparams={k: d})
+        print(f"  d elem field {k}: adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+        if ad == 0 and fd == 0:
+            continue   # no element at yield in this state
+        worst = max(worst, rel)
+    dv = np.zeros(capi.NBDRY)
+    dv[:2] = win.base_vbc[:2] * 1e-6
+    ad, fd, rel = _check(win, seed, dparams={"vbc_values": dv})
+    print(f"  d vbc_values: adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+    worst = max(worst, rel)
+    tseed = {"temperature": seed["temperature"]}
+    d = rng.standard_normal(ne) * 1e-3 * wl.mat.therm_cond[0]
+    ad, fd, rel = _check(win, tseed, dparams={capi.EF_THERM_COND: d})
+    print(f"  d therm_cond: adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+    worst = max(worst, rel)
+    assert worst <= 1e-6, worst
+
+
+def test_reverse_log10_viscosity():
+    """Per-element log10 viscosity replacing the viscosity law, 3 steps."""
+    from dynearthsol_gb300 import capi
+    rng = np.random.default_rng(3)
+    wl = _workload()
+    ne = wl.mesh.nelem
+    wl.elem_fields = {capi.EF_LOG10_VISC: 21 + 0.5 * rng.standard_normal(ne)}
+    win = _window(wl, 3, 2)
+    seed = _seed(win, rng)
+    seed = {"vel": seed["vel"], "stress": seed["stress"]}
+    d = rng.standard_normal(ne) * 1e-3
+    ad, fd, rel = _check(win, seed, dparams={capi.EF_LOG10_VISC: d})
+    print(f"  d log10 visc: adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+    assert rel <= 1e-5, rel
+
+
+def test_reverse_window_checkpointing_is_exact():
+    """The gradients do not depend on the checkpoint spacing (the recompute
+    is bit-reproducible), and match the central difference over 12 steps."""
+    rng = np.random.default_rng(4)
+    win = _window(_workload(), 12, 5)
+    seed = _seed(win, rng)
+    win.run()
+    s5, g5 = win.gradients(seed)
+    win.C = 12
+    win.run()
+    s12, g12 = win.gradients(seed)
+    for k in FIELDS:
+        np.testing.assert_array_equal(s5[k], s12[k], err_msg=k)
+    np.testing.assert_array_equal(g5["vbc_values"], g12["vbc_values"])
+    win.C = 5
+    for f in ("vel", "stress", "coord"):
+        ad, fd, rel = _check(win, seed, dstate=_dstate(win, rng, f))
+        print(f"  12 steps d{f:8s} adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+        assert rel <= 1e-5, (f, rel)
+
+
+def _yield_window(rt, K, C):
+    from dataclasses import replace
+    from cases import build_case
+    from dynearthsol_gb300 import capi
+    wl, _ = build_case("3d_evp_yield")
+    wl.params = replace(wl.params, damping_option=2)
+    wl.mat = replace(wl.mat, rheol_type=rt)
+    ne = wl.mesh.nelem
+    wl.elem_fields = {capi.EF_COHESION1: np.full(ne, wl.mat.cohesion1[0]),
+                      capi.EF_FRICTION1: np.full(ne, wl.mat.friction_angle1[0])}
+    win = _window(wl, K, C, spin=20)
+    final = win.run()
+    assert (final["plstrain"] > win.start["plstrain"] + 1e-12).sum() > 0, "no element yields"
+    return wl, win
+
+
+def test_reverse_yielding_elasto_plastic():
+    """Mohr-Coulomb return map active (elasto-plastic): start-state
+    directions over 3 steps, and the cohesion / friction-angle gradients of
+    the yielding elements (their plastic strain is past the softening
+    segment, so the saturated values act) over one step.  Over several
+    yielding steps the central difference of a parameter has a rounding floor
+    of ~1e-11 of the loss (eigen-solver rounding in the yielding elements),
+    above the 1e-10 signal of a random parameter direction."""
+    from dynearthsol_gb300 import capi
+    rng = np.random.default_rng(5)
+    rt = capi.RH_ELASTIC | capi.RH_PLASTIC
+    wl, win = _yield_window(rt, 3, 2)
+    ne = wl.mesh.nelem
+    seed = _seed(win, rng)
+    for f in ("vel", "stress", "coord"):
+        ad, fd, rel = _check(win, seed, dstate=_dstate(win, rng, f))
+        print(f"  EP d{f:8s} adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+        assert rel <= 1e-5, (f, rel)
+    wl, win = _yield_window(rt, 1, 1)
+    seed = _seed(win, rng)
+    for k, base in wl.elem_fields.items():
+        d = rng.standard_normal(ne) * 1e-6 * np.abs(base)
+        ad, fd, rel = _check(win, seed, dparams={k: d})
+        print(f"  EP d elem field {k}: adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+        assert ad != 0 and rel <= 1e-5, (k, ad, rel)
+
+
+def test_reverse_yielding_visco_elasto_plastic_one_step():
+    """The EVP branch choice with elements at yield, one step.  Over several
+    steps the choice of some elements flips within the finite-difference
+    perturbation, which the central difference then straddles."""
+    from dynearthsol_gb300 import capi
+    rng = np.random.default_rng(6)
+    wl, win = _yield_window(capi.RH_ELASTIC | capi.RH_VISCOUS | capi.RH_PLASTIC, 1, 1)
+    seed = _seed(win, rng)
+    for f in ("vel", "stress"):
+        ad, fd, rel = _check(win, seed, dstate=_dstate(win, rng, f))
+        print(f"  EVP d{f:8s} adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+        assert rel <= 1e-5, (f, rel)
+
+
+def test_reverse_matches_fp64_cpu_forward():
+    """The gradient of a top-surface velocity misfit with respect to the
+    per-element log10 viscosity (8 steps), against fourth-order central
+    differences of the CPU FP64 forward -- the oracle, the C restatement of
+    the reference -- run from the same start state with dt held (fixed_dt =
+    the window's dt).  h = 0.01: below that the differences of the
+    quasi-static velocity misfit are dominated by rounding, and a two-point
+    difference at that step carries a truncation error of ~3e-4."""
+    from dataclasses import replace
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.adjoint import fd5, surface_velocity_misfit, top_nodes
+    from oracle.oracle import Oracle, state_copy
+    rng = np.random.default_rng(8)
+    LV = capi.EF_LOG10_VISC
+    wl = _workload()
+    ne = wl.mesh.nelem
+    lv_t = 21 + 0.5 * rng.standard_normal(ne)
+    lv_s = 21 + 0.5 * rng.standard_normal(ne)
+    wl.elem_fields = {LV: lv_s}
+    K = 8
+    win = _window(wl, K, 4)
+    nodes = top_nodes(wl.mesh)
+    target = win.run({LV: lv_t})["vel"]
+    final = win.run({LV: lv_s})
+    loss, seed = surface_velocity_misfit(final["vel"], target, nodes)
+    _, g = win.gradients({"vel": seed})
+    g = g[LV]
+    win.m.upload(win.start, win.clock)
+    full = win.m.download()   # the start state with its derived fields
+    wl_cpu = replace(wl, params=replace(wl.params, fixed_dt=win.clock[1]))
+
+    def cpu_loss(lv):
+        st = state_copy(full)
+        wl_cpu.elem_fields = {LV: lv}
+        o = Oracle(wl_cpu, st, win.m.comp_pressure, 1, win.clock)
+        assert o.run(K) == 0
+        return surface_velocity_misfit(st["vel"], target, nodes)[0]
+
+    assert abs(cpu_loss(lv_s) - loss) <= 1e-9 * loss   # the two forwards agree
+    worst = 0.0
+    for e in np.argsort(-np.abs(g))[:6]:
+        def along(t, e=e):
+            lv = lv_s.copy()
+            lv[e] += t
+            return cpu_loss(lv)
+        fd = fd5(along, 1e-2)
+        rel = abs(fd - g[e]) / max(abs(fd), abs(g[e]))
+        print(f"  elem {e:4d}: adjoint {g[e]: .9e}  cpu fd {fd: .9e}  rel {rel:.2e}")
+        worst = max(worst, rel)
+    assert worst <= 1e-4, worst
