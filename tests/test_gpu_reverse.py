@@ -269,3 +269,39 @@ def test_reverse_matches_fp64_cpu_forward():
         print(f"  elem {e:4d}: adjoint {g[e]: .9e}  cpu fd {fd: .9e}  rel {rel:.2e}")
         worst = max(worst, rel)
     assert worst <= 1e-4, worst
+
+
+def test_reverse_torch_autograd_function():
+    """The torch.autograd.Function wrapper: a misfit built in torch from the
+    window's final velocities, loss.backward() through the adjoint; its
+    gradients equal the adjoint's and match a central difference."""
+    torch = pytest.importorskip("torch")
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.adjoint import fd5, top_nodes, window_function
+    rng = np.random.default_rng(9)
+    wl = _workload()
+    ne = wl.mesh.nelem
+    lv0 = 21 + 0.5 * rng.standard_normal(ne)
+    wl.elem_fields = {capi.EF_LOG10_VISC: lv0, capi.EF_SHEAR_MODULUS: np.full(ne, wl.mat.shear_modulus[0])}
+    win = _window(wl, 6, 3)
+    WF = window_function()
+    nodes = torch.from_numpy(top_nodes(wl.mesh))
+    target = torch.from_numpy(win.run({capi.EF_LOG10_VISC: lv0 + 0.3})["vel"])
+
+    def loss_fn(lv, G):
+        v = WF.apply(win, lv, G, None, None, None, None, None, None)
+        return 0.5 * ((v[nodes] - target[nodes]) ** 2).sum()
+
+    lv = torch.tensor(lv0, dtype=torch.float64, requires_grad=True)
+    G = torch.tensor(wl.elem_fields[capi.EF_SHEAR_MODULUS], dtype=torch.float64, requires_grad=True)
+    loss = loss_fn(lv, G)
+    loss.backward()
+    d_lv = rng.standard_normal(ne) * 1e-2
+    d_G = rng.standard_normal(ne) * 1e-3 * float(wl.mat.shear_modulus[0])
+    ad = float(lv.grad.numpy() @ d_lv + G.grad.numpy() @ d_G)
+    with torch.no_grad():
+        fd = fd5(lambda t: float(loss_fn(torch.from_numpy(lv0 + t * d_lv),
+                                         torch.from_numpy(G.detach().numpy() + t * d_G))), 1.0)
+    rel = abs(fd - ad) / max(abs(fd), abs(ad))
+    print(f"  autograd: adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
+    assert rel <= 1e-5, rel
