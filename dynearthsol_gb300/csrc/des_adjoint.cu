@@ -712,6 +712,11 @@ __device__ void mc_return_reverse(double K, double G, double amc, double anphi, 
                                   double &gG, double &gamc, double &ganphi, double &ganpsi, double &ghardn,
                                   double &gtmax)
 {
+    if (clearly_elastic3(amc, anphi, tmax, S)) {   // S' = S (the forward skipped the eigen-solve too)
+#pragma unroll
+        for (int cc = 0; cc < 6; ++cc) gS[cc] += go[cc];
+        return;
+    }
     double pr[3], v[3][3];
     principal_stresses3(S, pr, v);
     const double fs = pr[0] - pr[2] * anphi + amc;
@@ -893,7 +898,7 @@ __global__ void __launch_bounds__(TPB_A) k_adj_stress(KP p, AdjBufs a, TapeStep 
             }
             maxwell_<3>(K, G, visc, dt, dv, de, sv);
             double depls;
-            mc_return_<3>(K, G, amc, anphi, anpsi, hardn, tmax, depls, sp);
+            if (!clearly_elastic3(amc, anphi, tmax, sp)) mc_return_<3>(K, G, amc, anphi, anpsi, hardn, tmax, depls, sp);
             plastic = !(second_invariant2_<3>(sv) < second_invariant2_<3>(sp));
         }
         if (plastic) {

@@ -42,73 +42,6 @@ static inline int nblocks_m(long long n)
     return (int)(b < 1 ? 1 : b);
 }
 
-// ------------------------------------------------------------------
-// FP32 cyclic Jacobi for a symmetric 3x3 matrix (Jacobi 1846; the stable
-// rotation formulas of Rutishauser, as in Golub & Van Loan, "Matrix
-// Computations", sec. 8.5).  Fixed sweep count: no data-dependent branches
-// besides skipping exact zeros.  v[r][k] is component r of eigenvector k.
-// ------------------------------------------------------------------
-template <int P, int Q>
-__device__ __forceinline__ void jrot(float (&a)[3][3], float (&v)[3][3])
-{
-    constexpr int R = 3 - P - Q;
-    const float apq = a[P][Q];
-    if (apq == 0.0f) return;
-    const float theta = __fdividef(a[Q][Q] - a[P][P], 2.0f * apq);
-    // |theta| -> inf (negligible apq) gives t = 0: no rotation
-    const float at = fabsf(theta);
-    const float t = copysignf(__frcp_rn(at + __fsqrt_rn(fmaf(at, at, 1.0f))), theta);
-    const float c = rsqrtf(fmaf(t, t, 1.0f));
-    const float s = t * c;
-    const float tau = __fdividef(s, 1.0f + c);
-    a[P][P] -= t * apq;
-    a[Q][Q] += t * apq;
-    a[P][Q] = a[Q][P] = 0.0f;
-    const float arp = a[R][P], arq = a[R][Q];
-    a[R][P] = a[P][R] = arp - s * (arq + tau * arp);
-    a[R][Q] = a[Q][R] = arq + s * (arp - tau * arq);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float vkp = v[k][P], vkq = v[k][Q];
-        v[k][P] = vkp - s * (vkq + tau * vkp);
-        v[k][Q] = vkq + s * (vkp - tau * vkq);
-    }
-}
-
-// eigenvalues ascending in w, eigenvectors in the columns of v
-__device__ __forceinline__ void jacobi3f(const float d[6], float w[3], float (&v)[3][3])
-{
-    float a[3][3] = {{d[0], d[3], d[4]}, {d[3], d[1], d[5]}, {d[4], d[5], d[2]}};
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? 1.0f : 0.0f;
-#pragma unroll
-    for (int sweep = 0; sweep < 4; ++sweep) {
-        jrot<0, 1>(a, v);
-        jrot<0, 2>(a, v);
-        jrot<1, 2>(a, v);
-    }
-    w[0] = a[0][0];
-    w[1] = a[1][1];
-    w[2] = a[2][2];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const int i = (k == 1) ? 1 : 0, j = i + 1;
-        if (w[i] > w[j]) {
-            float t = w[i];
-            w[i] = w[j];
-            w[j] = t;
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                float b = v[r][i];
-                v[r][i] = v[r][j];
-                v[r][j] = b;
-            }
-        }
-    }
-}
-
 // Arrhenius power-law viscosity (matprops.cxx:276-312) for nmat == 1:
 //   ln visc = ln(0.25e6 coef) + pw ln(edot_II) + Q / (n R T),
 // with every term kept to ~1e-8 absolute at ~10 FP64 operations:
@@ -138,34 +71,6 @@ __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *e
     const double k = rint(lnv * INV_LN2);
     const float rr = (float)(lnv - k * LN2);
     return ldexp((double)expf(rr), (int)k);
-}
-
-// Screen of the Mohr-Coulomb yield test (rheology.cxx:163-178) in FP32.
-// The deviatoric trial stress D is diagonalised in FP32 (eigenvalues only);
-// the principal stresses and yield functions are formed in FP64 from the
-// FP64 mean stress.  Each computed eigenvalue lies within ||E||_2 of the
-// exact one (Weyl), E being the backward error of rounding D to FP32 and of
-// twelve Jacobi rotations: a few tens of eps32 ||D||_F.  The screen passes
-// an element only when both yield functions clear the surface by the margin
-// tol = 2^-12 ||D||_F (~4000 eps32 ||D||_F); every other element takes the
-// FP64 return map, so whatever yields follows the FP64 path exactly --
-// including the choice of principal directions when two principal stresses
-// (nearly) coincide, which FP32 cannot resolve and which decides the
-// direction of the plastic correction.
-__device__ __forceinline__ bool clearly_elastic_mixed(double amc, double anphi, double ten_max, const double *s)
-{
-    const double m = (s[0] + s[1] + s[2]) * (1.0 / 3);
-    const float d[6] = {(float)(s[0] - m), (float)(s[1] - m), (float)(s[2] - m),
-                        (float)s[3], (float)s[4], (float)s[5]};
-    float w[3], v[3][3];
-    jacobi3f(d, w, v);
-    const float nf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
-                           + 2.0f * (d[3] * d[3] + d[4] * d[4] + d[5] * d[5]));
-    const double tol = (double)nf * (1.0 / 4096);
-    const double p0 = m + (double)w[0], p2 = m + (double)w[2];
-    const double fs = p0 - p2 * anphi + amc;
-    const double ft = p2 - ten_max;
-    return fs > (1 + anphi) * tol && ft < -tol;
 }
 
 // maxwell (rheology.cxx:118-134) with 1/viscosity and 1/(1+tmp) by
@@ -248,7 +153,7 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
         for (int i = 0; i < 6; ++i) sp[i] = s[i];
         elastic_<3>(bulkm, shearm, de, sp);
         double depls = 0;
-        if (!clearly_elastic_mixed(amc, anphi, ten_max, sp) &&
+        if (!clearly_elastic3(amc, anphi, ten_max, sp) &&
             mc_return_<3>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp))
             bits |= DES_DEV_QL_NOCONV;
         if (rt == DES_RH_EP) {

@@ -274,6 +274,103 @@ __device__ __forceinline__ void viscous_(double bulkm, double viscosity, double 
     for (int i = ND; i < NSTR; ++i) s[i] = 2 * viscosity * edot[i];
 }
 
+// ------------------------------------------------------------------
+// FP32 cyclic Jacobi for a symmetric 3x3 matrix (Jacobi 1846; the stable
+// rotation formulas of Rutishauser, as in Golub & Van Loan, "Matrix
+// Computations", sec. 8.5).  Fixed sweep count: no data-dependent branches
+// besides skipping exact zeros.  v[r][k] is component r of eigenvector k.
+// ------------------------------------------------------------------
+template <int P, int Q>
+__device__ __forceinline__ void jrot(float (&a)[3][3], float (&v)[3][3])
+{
+    constexpr int R = 3 - P - Q;
+    const float apq = a[P][Q];
+    if (apq == 0.0f) return;
+    const float theta = __fdividef(a[Q][Q] - a[P][P], 2.0f * apq);
+    // |theta| -> inf (negligible apq) gives t = 0: no rotation
+    const float at = fabsf(theta);
+    const float t = copysignf(__frcp_rn(at + __fsqrt_rn(fmaf(at, at, 1.0f))), theta);
+    const float c = rsqrtf(fmaf(t, t, 1.0f));
+    const float s = t * c;
+    const float tau = __fdividef(s, 1.0f + c);
+    a[P][P] -= t * apq;
+    a[Q][Q] += t * apq;
+    a[P][Q] = a[Q][P] = 0.0f;
+    const float arp = a[R][P], arq = a[R][Q];
+    a[R][P] = a[P][R] = arp - s * (arq + tau * arp);
+    a[R][Q] = a[Q][R] = arq + s * (arp - tau * arq);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float vkp = v[k][P], vkq = v[k][Q];
+        v[k][P] = vkp - s * (vkq + tau * vkp);
+        v[k][Q] = vkq + s * (vkp - tau * vkq);
+    }
+}
+
+// eigenvalues ascending in w, eigenvectors in the columns of v
+__device__ __forceinline__ void jacobi3f(const float d[6], float w[3], float (&v)[3][3])
+{
+    float a[3][3] = {{d[0], d[3], d[4]}, {d[3], d[1], d[5]}, {d[4], d[5], d[2]}};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? 1.0f : 0.0f;
+#pragma unroll
+    for (int sweep = 0; sweep < 4; ++sweep) {
+        jrot<0, 1>(a, v);
+        jrot<0, 2>(a, v);
+        jrot<1, 2>(a, v);
+    }
+    w[0] = a[0][0];
+    w[1] = a[1][1];
+    w[2] = a[2][2];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int i = (k == 1) ? 1 : 0, j = i + 1;
+        if (w[i] > w[j]) {
+            float t = w[i];
+            w[i] = w[j];
+            w[j] = t;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                float b = v[r][i];
+                v[r][i] = v[r][j];
+                v[r][j] = b;
+            }
+        }
+    }
+}
+
+// Screen of the Mohr-Coulomb yield test (rheology.cxx:163-178) in FP32, for
+// 3D.  The deviatoric trial stress D is diagonalised in FP32 (eigenvalues
+// only); the principal stresses and yield functions are formed in FP64 from
+// the FP64 mean stress m.  Each computed eigenvalue lies within ||E||_2 of
+// the exact one (Weyl), E being the backward error of rounding D to FP32 and
+// of twelve Jacobi rotations: a few tens of eps32 ||D||_F.  The FP64
+// principal stresses of the full stress (principal_stresses3) carry errors
+// of a few eps64 (|m| + ||D||).  The screen passes an element only when both
+// yield functions clear the surface by tol = 2^-12 ||D||_F + 2^-40 |m|
+// (~4000 eps32 ||D||_F plus ~200 times the FP64 error in |m|), so a passed
+// element is elastic in the FP64 test too: its output is its trial stress,
+// bit for bit, and the eigen-solve is skipped.  Every other element takes
+// the FP64 return map, including the choice of principal directions when
+// two principal stresses (nearly) coincide, which FP32 cannot resolve.
+__device__ __forceinline__ bool clearly_elastic3(double amc, double anphi, double ten_max, const double *s)
+{
+    const double m = (s[0] + s[1] + s[2]) * (1.0 / 3);
+    const float d[6] = {(float)(s[0] - m), (float)(s[1] - m), (float)(s[2] - m),
+                        (float)s[3], (float)s[4], (float)s[5]};
+    float w[3], v[3][3];
+    jacobi3f(d, w, v);
+    const float nf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
+                           + 2.0f * (d[3] * d[3] + d[4] * d[4] + d[5] * d[5]));
+    const double tol = (double)nf * (1.0 / 4096) + 0x1p-40 * fabs(m);
+    const double p0 = m + (double)w[0], p2 = m + (double)w[2];
+    const double fs = p0 - p2 * anphi + amc;
+    const double ft = p2 - ten_max;
+    return fs > (1 + anphi) * tol && ft < -tol;
+}
+
 // Mohr-Coulomb return map in principal space of the elastic trial stress s
 // (rheology.cxx:163-299).  Returns nonzero when the QL fallback of the
 // eigen-solver hit its sweep cap.
@@ -338,12 +435,18 @@ __device__ int mc_return_(double bulkm, double shearm, double amc, double anphi,
     return rc;
 }
 
-// elasto_plastic (rheology.cxx:151-299): elastic trial stress, then the return map
+// elasto_plastic (rheology.cxx:151-299): elastic trial stress, then the
+// return map; in 3D the FP32 screen first skips the eigen-solve of the
+// elements that are elastic beyond its error bound (same result, bit for bit)
 template <int ND>
 __device__ int elasto_plastic_(double bulkm, double shearm, double amc, double anphi, double anpsi,
                                double hardn, double ten_max, const double *de, double &depls, double *s)
 {
     elastic_<ND>(bulkm, shearm, de, s);
+    if (ND == 3 && clearly_elastic3(amc, anphi, ten_max, s)) {
+        depls = 0;
+        return 0;
+    }
     return mc_return_<ND>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, s);
 }
 
