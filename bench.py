@@ -299,6 +299,8 @@ def main():
                     help="elements checked against central differences in the adjoint benchmark")
     ap.add_argument("--heat-adjoint-steps", type=int, default=200,
                     help="window of the heat adjoint on the 4,056,000-tet jittered mesh (0: skip)")
+    ap.add_argument("--scale-steps", type=int, default=1000,
+                    help="steps of the 7,987,200-tet mixed-vs-FP64 run (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -379,6 +381,9 @@ def main():
     heat_adjoint = None
     if args.heat_adjoint_steps > 0 and rank == 0:
         heat_adjoint = heat_adjoint_bench(args, stream)
+    scale = None
+    if args.scale_steps > 0 and rank == 0:
+        scale = scale_bench(args, stream)
     if rank == 0:
         line = {
             "metric": metric_name(args), "value": value, "unit": "Mtet-steps/s", "n_gpus": world,
@@ -395,6 +400,7 @@ def main():
             "e2e": e2e,
             "adjoint": adjoint,
             "heat_adjoint": heat_adjoint,
+            "scale": scale,
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
@@ -498,6 +504,56 @@ def adjoint_bench(args, stream):
             "fd_gradient_direction": gdir,
             "dt": "held at the start value (compute_dt not called in the window)",
             "damping_option": 2}
+
+
+def scale_bench(args, stream):
+    """The mixed step at scale: 7,987,200 tets (160x160x52 cubes x6), the 3D
+    EVP physics with per-element cohesion0/1 x (1 + 0.05 N(0,1)), seeded;
+    `scale_steps` steps of the mixed and of the FP64 step from the same
+    state, each timed with CUDA events on the library's stream, and the
+    error of every field of the mixed run against the FP64 run."""
+    import torch
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import initial_state, make_workload
+    from dynearthsol_gb300.solver import DeviceModel
+    n = args.scale_steps
+    t0 = time.perf_counter()
+    wl = make_workload("c2_3d_evp_noise")
+    st, cp = initial_state(wl)
+    ne = wl.mesh.nelem
+    f = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_FP64, stream=stream.cuda_stream)
+    init = f.init_fields(st)
+    clk = f.clock()
+    mx = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_MIXED, stream=stream.cuda_stream)
+    mx.upload(init, clk)
+    t_setup = time.perf_counter() - t0
+    out = {}
+    for name, m in (("mixed", mx), ("fp64", f)):
+        m.step(2)
+        m.upload(init, clk)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        m.step(n)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"ms_per_step": ms / n, "value": ne * n / (ms / 1e3) / 1e6}
+    a, b = f.download(), mx.download()
+    fields = ("vel", "stress", "strain", "temperature", "plstrain", "coord", "force", "volume")
+    errs = {}
+    for k in fields:
+        den = float(np.abs(a[k]).max()) or 1.0
+        errs[k] = float(np.abs(b[k] - a[k]).max()) / den
+    l2 = float(np.linalg.norm(b["stress"] - a["stress"]) / np.linalg.norm(a["stress"]))
+    yielded = int((a["plstrain"] > init["plstrain"] + 1e-12).sum())
+    f.close()
+    mx.close()
+    return {"workload": "c2_3d_evp_noise", "nelem": ne, "steps": n, "mixed": out["mixed"], "fp64": out["fp64"],
+            "speedup_mixed_over_fp64": out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"],
+            "stress_rel_l2_err_vs_fp64": l2, "max_normalised_err_vs_fp64": errs,
+            "yielded_elements_fp64": yielded, "damping_option": wl.params.damping_option,
+            "host_setup_s": t_setup}
 
 
 def heat_adjoint_bench(args, stream):
