@@ -143,6 +143,17 @@ class DesAdjointGrad(C.Structure):
     _fields_ = [("elem", _dp * EF_COUNT), ("vbc_values", C.c_double * NBDRY)]
 
 
+SAVE_FIELDS = ("coord", "connectivity", "vel", "temperature", "plstrain", "delta_plstrain", "strain_rate",
+               "strain", "stress", "density", "mesh_quality", "viscosity", "material", "force", "coord0",
+               "bcflag")
+
+
+class DesSaveFrame(C.Structure):
+    """des_save_frame: host arrays of one .save output frame."""
+    _fields_ = [("ndims", C.c_int), ("nnode", C.c_int), ("nelem", C.c_int)] + [
+        (name, _ip if name == "connectivity" else (_up if name == "bcflag" else _dp)) for name in SAVE_FIELDS]
+
+
 def dptr(a: np.ndarray | None):
     """double* of a C-contiguous float64 array (NULL for None)."""
     if a is None:
@@ -212,6 +223,8 @@ _SIGS = {
     "des_synchronize": [C.c_void_p],
     "des_launch_count": [C.c_void_p, C.POINTER(C.c_longlong)],
     "des_nmd_stress_noalloc": [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 8,
+    "des_write_save_host": [C.c_char_p, C.POINTER(DesSaveFrame)],
+    "des_write_save": [C.c_void_p, C.c_char_p],
     "des_adjoint_forward": [C.c_void_p, C.c_int, C.c_int],
     "des_adjoint_backward": [C.c_void_p, C.POINTER(DesHostState), C.POINTER(DesHostState),
                              C.POINTER(DesAdjointGrad)],
@@ -268,3 +281,21 @@ def host_state_struct(st: dict, time: float = 0.0, dt: float = 0.0, steps: int =
     s.dt = dt
     s.steps = steps
     return s
+
+
+def read_save(path: str) -> dict:
+    """Read a .save frame (BinaryOutput layout, binaryio.cxx:16-37): a 4096-byte
+    header of "name<TAB>offset" lines after the revision line, then the arrays.
+    Returns {"ndims": n, name: flat array}; connectivity int32, bcflag uint32,
+    the rest float64."""
+    raw = open(path, "rb").read()
+    head = raw[:4096].split(b"\0", 1)[0].decode()
+    lines = head.splitlines()
+    ndims = int(lines[0].split("ndims=")[1].split()[0])
+    items = [(ln.rsplit("\t", 1)[0], int(ln.rsplit("\t", 1)[1])) for ln in lines[1:] if "\t" in ln]
+    out = {"ndims": ndims, "_order": [n for n, _ in items]}
+    for k, (name, off) in enumerate(items):
+        end = items[k + 1][1] if k + 1 < len(items) else len(raw)
+        dt = np.int32 if name == "connectivity" else (np.uint32 if name == "bcflag" else np.float64)
+        out[name] = np.frombuffer(raw[off:end], dtype=dt)
+    return out

@@ -765,6 +765,34 @@ __device__ __forceinline__ double elem_quality(const KP &p, int e)
 }
 
 // red[0] = min quality bits (quality > 0), red[1] = smallest index at that minimum
+
+// per-element fields of an output frame (output.cxx:146-173): density
+// (MatProps::rho), mesh quality (elem_quality), viscosity (MatProps::visc of
+// the current strain rate) and the most abundant marker's material
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_output_elem(KP p, double *out)
+{
+    constexpr int NSTR = ND * (ND + 1) / 2;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    const size_t ne = p.ne;
+    double edot[NSTR];
+#pragma unroll
+    for (int c = 0; c < NSTR; ++c) edot[c] = p.srate[c * ne + e];
+    out[e] = m_rho<ND>(p, e);
+    out[ne + e] = elem_quality<ND>(p, e);
+    out[2 * ne + e] = m_visc<ND>(p, e, edot);
+    int best = 0, bc = -1;
+    for (int m = 0; m < p.mat.nmat; ++m) {
+        const int k = mcount(p, e, m);
+        if (k > bc) {   // std::max_element: the first of equal maxima
+            bc = k;
+            best = m;
+        }
+    }
+    out[3 * ne + e] = best;
+}
+
 template <int ND>
 __global__ void __launch_bounds__(TPB) k_quality_min(KP p, unsigned long long *red)
 {
@@ -951,6 +979,12 @@ int launch_dt_finalize(const KP &p, cudaStream_t s, bool only_on_step)
 int launch_dt_reset(const KP &p, cudaStream_t s)
 {
     k_dt_reset<<<1, 1, 0, s>>>(p);
+    return 1;
+}
+
+int launch_output_elem(const KP &p, double *out, cudaStream_t s)
+{
+    DISPATCH(k_output_elem, nblocks(p.ne), p, out);
     return 1;
 }
 

@@ -36,6 +36,8 @@ int launch_geometry(const KP &p, cudaStream_t s, int flags);
 int launch_mass(const KP &p, cudaStream_t s);
 int launch_dt_finalize(const KP &p, cudaStream_t s, bool only_on_step);
 int launch_quality(const KP &p, cudaStream_t s, unsigned long long *red);
+// out[4][ne]: density, mesh quality, viscosity, material of an output frame
+int launch_output_elem(const KP &p, double *out, cudaStream_t s);
 int launch_dt_reset(const KP &p, cudaStream_t s);
 // material constants: visc_coef[nmat], then 4 values per plastic table entry
 int launch_material_table(const KP &p, cudaStream_t s, double *out);

@@ -275,6 +275,43 @@ int des_step(des_ctx *ctx, int nsteps);
  * This is the drop-in form for a caller whose Variables stay authoritative. */
 int des_step_host(des_ctx *ctx, des_host_state *st, int nsteps);
 
+/* ---- output frames in the reference's .save format ---------------------
+ * Output::write (output.cxx:79-195, not averaged, no marker output) with
+ * BinaryOutput's layout (binaryio.cxx:16-37): a 4096-byte ASCII header --
+ * "# DynEarthSol ndims=N revision=3\n" then one "name\tbyte offset\n" line
+ * per array -- followed by the arrays in the reference's row-major layout.
+ * Arrays, in order: coordinate, connectivity (int32), velocity,
+ * temperature, plastic strain, plastic strain-rate (delta_plstrain),
+ * strain-rate, strain, stress, density, mesh quality, viscosity, material
+ * (as doubles), force, coord0, bcflag (uint32). */
+typedef struct des_save_frame {
+    int ndims, nnode, nelem;
+    const double *coord;            /* [nnode][ndims] */
+    const int *connectivity;        /* [nelem][ndims+1] */
+    const double *vel;              /* [nnode][ndims] */
+    const double *temperature;      /* [nnode] */
+    const double *plstrain;         /* [nelem] */
+    const double *delta_plstrain;   /* [nelem] */
+    const double *strain_rate;      /* [nelem][nstr] */
+    const double *strain;           /* [nelem][nstr] */
+    const double *stress;           /* [nelem][nstr] */
+    const double *density;          /* [nelem] MatProps::rho */
+    const double *mesh_quality;     /* [nelem] elem_quality */
+    const double *viscosity;        /* [nelem] MatProps::visc */
+    const double *material;         /* [nelem] index of the most abundant marker's material */
+    const double *force;            /* [nnode][ndims] */
+    const double *coord0;           /* [nnode][ndims] */
+    const unsigned *bcflag;         /* [nnode] */
+} des_save_frame;
+
+/* Write one frame from host arrays (no device work). */
+int des_write_save_host(const char *filename, const des_save_frame *frame);
+/* Write the context's current state as one frame: density, mesh quality,
+ * viscosity and material are evaluated on the device, and only the frame's
+ * arrays come to the host.  Replaces Output::write (output.cxx:79-195) for
+ * a device-resident run; the caller names the file ("%s.save.%06d"). */
+int des_write_save(des_ctx *ctx, const char *filename);
+
 /* ---- reverse mode: the adjoint of a window of steps --------------------
  * No counterpart in the reference.  Gradients of a scalar loss of the
  * state after a window of nsteps steps of the 3D FP64 step, taken with dt

@@ -22,6 +22,7 @@
 #include "rheology.hpp"
 #include "bc.hpp"
 #include "ic.hpp"
+#include "binaryio.hpp"
 
 #include "../include/desgpu.h"
 
@@ -398,6 +399,51 @@ int ref_call(const des_mesh *mesh, const des_params *dp, const des_material *dm,
         result[1] = worst;
     } else return 1;
     state_out(var, st);
+    return 0;
+}
+
+/* One output frame written by the reference's BinaryOutput (binaryio.cxx),
+ * with the array names, types and order of Output::write
+ * (output.cxx:93-179, not averaged, no markers): the pin of the library's
+ * .save writer (des_write_save_host). */
+int ref_write_save(const char *filename, const des_save_frame *fr)
+{
+    if (fr->ndims != NDIMS) return 1;
+    const int nn = fr->nnode, ne = fr->nelem;
+    BinaryOutput bin(filename);
+    array_t coord(nn), vel(nn), force(nn), coord0(nn);
+    conn_t conn(ne);
+    tensor_t srate(ne), strain(ne), stress(ne);
+    std::memcpy(coord.data(), fr->coord, sizeof(double) * nn * NDIMS);
+    std::memcpy(vel.data(), fr->vel, sizeof(double) * nn * NDIMS);
+    std::memcpy(force.data(), fr->force, sizeof(double) * nn * NDIMS);
+    std::memcpy(coord0.data(), fr->coord0, sizeof(double) * nn * NDIMS);
+    std::memcpy(conn.data(), fr->connectivity, sizeof(int) * ne * NODES_PER_ELEM);
+    std::memcpy(srate.data(), fr->strain_rate, sizeof(double) * ne * NSTR);
+    std::memcpy(strain.data(), fr->strain, sizeof(double) * ne * NSTR);
+    std::memcpy(stress.data(), fr->stress, sizeof(double) * ne * NSTR);
+    double_vec T(fr->temperature, fr->temperature + nn), pls(fr->plstrain, fr->plstrain + ne),
+        dpls(fr->delta_plstrain, fr->delta_plstrain + ne), rho(fr->density, fr->density + ne),
+        quality(fr->mesh_quality, fr->mesh_quality + ne), visc(fr->viscosity, fr->viscosity + ne),
+        material(fr->material, fr->material + ne);
+    uint_vec bcflag(fr->bcflag, fr->bcflag + nn);
+    bin.write_array(coord, "coordinate", coord.size());
+    bin.write_array(conn, "connectivity", conn.size());
+    bin.write_array(vel, "velocity", vel.size());
+    bin.write_array(T, "temperature", T.size());
+    bin.write_array(pls, "plastic strain", pls.size());
+    bin.write_array(dpls, "plastic strain-rate", dpls.size());
+    bin.write_array(srate, "strain-rate", srate.size());
+    bin.write_array(strain, "strain", strain.size());
+    bin.write_array(stress, "stress", stress.size());
+    bin.write_array(rho, "density", rho.size());
+    bin.write_array(quality, "mesh quality", quality.size());
+    bin.write_array(visc, "viscosity", visc.size());
+    bin.write_array(material, "material", material.size());
+    bin.write_array(force, "force", force.size());
+    bin.write_array(coord0, "coord0", coord0.size());
+    bin.write_array(bcflag, "bcflag", bcflag.size());
+    bin.close();
     return 0;
 }
 
