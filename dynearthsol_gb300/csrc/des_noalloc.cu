@@ -20,7 +20,7 @@
 
 namespace {
 
-// per-node scratch: DES_NOALLOC_MAX_NODES doubles (8 MiB per device)
+// per-node scratch: DES_NOALLOC_MAX_NODES doubles (16 MiB per device)
 __device__ __align__(256) double g_nmd_scratch[DES_NOALLOC_MAX_NODES];
 
 constexpr int kMaxDevices = 64;
