@@ -307,6 +307,8 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
         add((void **)&d_qv, (size_t)ne * D);
     }
     add((void **)&c->d_rho, (size_t)ne * D);
+    add((void **)&p.me, (size_t)ne * D);
+    add((void **)&p.tme, (size_t)ne * D);
     add((void **)&p.fv, (size_t)std::max(nbf, 1) * nd * D);
     add((void **)&p.clk, sizeof(Clock));
     add((void **)&p.err, sizeof(unsigned));
@@ -878,10 +880,10 @@ int enqueue_step_mixed(des_ctx *c)
     n += launch_nmd_gather(p, s);
     n += launch_nmd_correct(p, s, true);
     n += launch_force(p, s, true);
-    int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP;
+    int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP | GEO_MASS_TERMS;
     if (p.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;   // FP32 increments in a mixed context
     n += launch_geometry(p, s, geo);
-    n += launch_mass(p, s);
+    n += launch_mass_sum(p, s);
     n += launch_dt_finalize(p, s, true);
     return n;
 }
@@ -904,10 +906,10 @@ int enqueue_step(des_ctx *c)
     n += launch_nmd_gather(p, s);
     n += launch_nmd_correct(p, s, true);
     n += launch_force(p, s, true);
-    int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP;
+    int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP | GEO_MASS_TERMS;
     if (p.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;
     n += launch_geometry(p, s, geo);
-    n += launch_mass(p, s);
+    n += launch_mass_sum(p, s);
     n += launch_dt_finalize(p, s, true);
     return n;
 }

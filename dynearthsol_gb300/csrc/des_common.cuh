@@ -97,6 +97,7 @@ struct KP {
     float *shp32;                        // FP32 copy of shp for the mixed step, or null
     float *hc;                           // [4][ne] per-element heat terms of the mixed step, or null
     double *qv;                          // [ne] per-element dvoldt term of the mixed step, or null
+    double *me, *tme;                    // [ne] per-element mass and tmass terms of the fused step
     const double *ef[DES_EF_COUNT];      // per-element overrides or null
     Clock *clk;
     unsigned *err;
@@ -133,6 +134,14 @@ __device__ __forceinline__ double div3(double x)
     constexpr double YL = 0x1.5555555555555p-56;   // RN(1/3 - YH)
     if (fabs(x) < 0x1p-900) return x / 3;
     return fma(x, YH, x * YL);
+}
+
+// x / 6, bit-identical to the division: x * 0.5 is exact (x above the
+// subnormal range) and div3 rounds (x / 2) / 3 = x / 6 correctly
+__device__ __forceinline__ double div6(double x)
+{
+    if (fabs(x) < 0x1p-900) return x / 6;
+    return div3(x * 0.5);
 }
 
 // x / ND for ND = 2 or 3, bit-identical to the division
@@ -411,7 +420,7 @@ __device__ __forceinline__ double tet_volume(const double *d0, const double *d1,
     double x01 = d0[0] - d1[0], x12 = d1[0] - d2[0], x23 = d2[0] - d3[0];
     double y01 = d0[1] - d1[1], y12 = d1[1] - d2[1], y23 = d2[1] - d3[1];
     double z01 = d0[2] - d1[2], z12 = d1[2] - d2[2], z23 = d2[2] - d3[2];
-    return (x01 * (y23 * z12 - y12 * z23) + x12 * (y01 * z23 - y23 * z01) + x23 * (y12 * z01 - y01 * z12)) / 6;
+    return div6(x01 * (y23 * z12 - y12 * z23) + x12 * (y01 * z23 - y23 * z01) + x23 * (y12 * z01 - y01 * z12));
 }
 
 // triangle_area (geometry.cxx:53-83)

@@ -639,6 +639,16 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
                 p.strain[cc * ne + e] = es[cc];
             }
         }
+        if (flags & GEO_MASS_TERMS) {
+            // compute_mass element terms (geometry.cxx:313-365), as k_mass forms them
+            const double rho_e = p.rho_e ? p.rho_e[e] : m_rho<ND>(p, e);
+            const double pseudo_speed = p.prm.max_vbc_val * p.prm.inertial_scaling;
+            const double rho = p.prm.is_quasi_static
+                ? ((p.mat.nmat == 1) ? p.mat.rho_pseudo : m_bulkm(p, e) / (pseudo_speed * pseudo_speed))
+                : rho_e;
+            p.me[e] = rho * vol / NPE;
+            if (p.prm.has_thermal_diffusion) p.tme[e] = rho_e * m_cp(p, e) * vol / NPE;
+        }
         if (do_dt) {
             // compute_dt element terms (geometry.cxx:254-292)
             double minh;
@@ -728,6 +738,26 @@ __global__ void __launch_bounds__(TPB) k_mass(KP p)
         vn += vol;
         ms += m;
         if (thermal) tm += rho_e * m_cp(p, e) * vol / NPE;
+    }
+    p.vol_n[n] = vn;
+    p.mass[n] = ms;
+    p.tmass[n] = tm;
+}
+
+// the node sums of compute_mass from the element terms that the geometry
+// pass wrote (GEO_MASS_TERMS): per pair 3 additions instead of the terms
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_mass_sum(KP p)
+{
+    int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.nn) return;
+    const bool thermal = p.prm.has_thermal_diffusion;
+    double vn = 0, ms = 0, tm = 0;
+    for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+        int e = p.sup_ent[q] >> 2;
+        vn += p.vol[e];
+        ms += p.me[e];
+        if (thermal) tm += p.tme[e];
     }
     p.vol_n[n] = vn;
     p.mass[n] = ms;
@@ -966,6 +996,12 @@ int launch_geometry(const KP &p, cudaStream_t s, int flags)
 int launch_mass(const KP &p, cudaStream_t s)
 {
     DISPATCH(k_mass, nblocks(p.nn), p);
+    return 1;
+}
+
+int launch_mass_sum(const KP &p, cudaStream_t s)
+{
+    DISPATCH(k_mass_sum, nblocks(p.nn), p);
     return 1;
 }
 

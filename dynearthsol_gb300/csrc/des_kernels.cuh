@@ -14,7 +14,8 @@ enum GeoFlags : int {
     GEO_SHAPE = 4,       // compute_shape_fn            (geometry.cxx:368-455)
     GEO_ROTATE = 8,      // rotate_stress               (fields.cxx:411-483)
     GEO_DT = 16,         // compute_dt element terms    (geometry.cxx:254-292)
-    GEO_DT_IF_STEP = 32  // ... only when steps % 10 == 0 (dynearthsol.cxx:349-361)
+    GEO_DT_IF_STEP = 32, // ... only when steps % 10 == 0 (dynearthsol.cxx:349-361)
+    GEO_MASS_TERMS = 64  // the element's mass and tmass terms -> me, tme (for launch_mass_sum)
 };
 
 // Each launcher returns the number of kernels it launched.
@@ -34,6 +35,8 @@ int launch_vbcs(const KP &p, cudaStream_t s);
 int launch_coordinate(const KP &p, cudaStream_t s);
 int launch_geometry(const KP &p, cudaStream_t s, int flags);
 int launch_mass(const KP &p, cudaStream_t s);
+// compute_mass from the element terms of a GEO_MASS_TERMS geometry pass (same sums, same order)
+int launch_mass_sum(const KP &p, cudaStream_t s);
 int launch_dt_finalize(const KP &p, cudaStream_t s, bool only_on_step);
 int launch_quality(const KP &p, cudaStream_t s, unsigned long long *red);
 // out[4][ne]: density, mesh quality, viscosity, material of an output frame

@@ -72,3 +72,16 @@ def test_div3_special_values():
     for x in (0.0, -0.0, math.inf, -math.inf, 2.0 ** -1074, -(2.0 ** -1000), 1.7976931348623157e308):
         assert _bits(_div3(x)) == _bits(x / 3), x
     assert math.isnan(_div3(math.nan))
+
+
+def _div6(x):
+    if abs(x) < 2.0 ** -900:
+        return x / 6
+    return _div3(x * 0.5)
+
+
+def test_div6_is_bit_identical_to_division():
+    """div6 = div3(x / 2): halving is exact above the subnormal range."""
+    xs = _inputs() + [math.ldexp(1.0, p) * 1.5 for p in range(-1074, -890)]
+    bad = [x for x in xs if _bits(_div6(x)) != _bits(x / 6)]
+    assert not bad, [x.hex() for x in bad[:10]]
