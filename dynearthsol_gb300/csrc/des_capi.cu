@@ -71,6 +71,10 @@ void invalidate_graph(des_ctx *c)
         cudaGraphExecDestroy(c->step_exec);
         c->step_exec = nullptr;
     }
+    if (c->step_exec_mid) {
+        cudaGraphExecDestroy(c->step_exec_mid);
+        c->step_exec_mid = nullptr;
+    }
 }
 
 void set_rho_pseudo(des_ctx *c);
@@ -442,6 +446,13 @@ int des_destroy(des_ctx *c)
     cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
     adj_free(c);
+    if (c->xstream) {
+        cudaStreamSynchronize(c->xstream);
+        cudaStreamDestroy(c->xstream);
+        for (cudaEvent_t e : c->xev) cudaEventDestroy(e);
+        cudaEventDestroy(c->ev_mid);
+        cudaFree(c->d_xstage);
+    }
     for (int k = 0; k < DES_EF_COUNT; ++k)
         if (c->d_ef[k]) cudaFree(c->d_ef[k]);
     cudaFree(c->pool);
@@ -519,6 +530,162 @@ int get_field(des_ctx *c, double *host, const double *dev, int n, int ncomp)
     return DES_OK;
 }
 
+// Pipelined state transfer.  The host rows of every field move by DMA on the
+// copy stream, back to back; a multi-component field lands in its own region
+// of the staging area and is converted between the reference's AoS rows and
+// the device SoA arrays on the compute stream while the next field's copy
+// runs.  Events order each conversion against its copy.  The host link is
+// then busy for the whole transfer (one DMA and one conversion per field,
+// serialised on one stream, left it idle during every conversion).
+int ensure_xfer(des_ctx *c)
+{
+    if (c->xstream) return DES_OK;
+    if (!c->d_xstage) {
+        const size_t need = (size_t)4 * c->nn * c->nd + (size_t)3 * c->ne * c->nstr + (size_t)c->nd * c->ne * c->npe;
+        CK(cudaMalloc((void **)&c->d_xstage, need * sizeof(double)));
+        c->xstage_doubles = need;
+    }
+    for (cudaEvent_t &e : c->xev)
+        if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (!c->ev_mid) CK(cudaEventCreateWithFlags(&c->ev_mid, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&c->xstream, cudaStreamNonBlocking));
+    return DES_OK;
+}
+
+// One direction of a pipelined transfer: begin(), field() per field, end().
+struct Pipe {
+    des_ctx *c;
+    bool up;
+    size_t off = 0;   // staging doubles handed out
+    int nev = 2;      // xev[0]: start, xev[1]: done, then one per converted field
+
+    // The copies start after what the compute stream has queued so far
+    // (or after `after`, an event of it).
+    int begin(cudaEvent_t after = nullptr)
+    {
+        if (!after) {
+            CK(cudaEventRecord(c->xev[0], c->stream));
+            after = c->xev[0];
+        }
+        CK(cudaStreamWaitEvent(c->xstream, after, 0));
+        return DES_OK;
+    }
+    // on_copy_stream: a download whose conversion runs on the copy stream
+    // (the compute stream is still busy with kernels that do not write `dev`)
+    int field(double *host, double *dev, int n, int ncomp, bool on_copy_stream = false)
+    {
+        const size_t cnt = (size_t)n * ncomp, bytes = cnt * sizeof(double);
+        if (cnt == 0) return DES_OK;
+        if (ncomp == 1) {
+            if (up) CK(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, c->xstream));
+            else CK(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->xstream));
+            return DES_OK;
+        }
+        if (off + cnt > c->xstage_doubles || nev >= DES_XFER_EVENTS)
+            return fail_msg(c->err, DES_EINPUT, "state transfer: a field was given twice");
+        double *stg = c->d_xstage + off;
+        off += cnt;
+        cudaEvent_t ev = c->xev[nev++];
+        int rc;
+        if (up) {
+            CK(cudaMemcpyAsync(stg, host, bytes, cudaMemcpyHostToDevice, c->xstream));
+            CK(cudaEventRecord(ev, c->xstream));
+            CK(cudaStreamWaitEvent(c->stream, ev, 0));
+            return check_launch(c, launch_aos_to_soa(stg, dev, n, ncomp, c->stream));
+        }
+        if (on_copy_stream) {
+            if ((rc = check_launch(c, launch_soa_to_aos(dev, stg, n, ncomp, c->xstream)))) return rc;
+        } else {
+            if ((rc = check_launch(c, launch_soa_to_aos(dev, stg, n, ncomp, c->stream)))) return rc;
+            CK(cudaEventRecord(ev, c->stream));
+            CK(cudaStreamWaitEvent(c->xstream, ev, 0));
+        }
+        CK(cudaMemcpyAsync(host, stg, bytes, cudaMemcpyDeviceToHost, c->xstream));
+        return DES_OK;
+    }
+    // the compute stream's later work waits for every copy
+    int end()
+    {
+        CK(cudaEventRecord(c->xev[1], c->xstream));
+        CK(cudaStreamWaitEvent(c->stream, c->xev[1], 0));
+        return DES_OK;
+    }
+};
+
+// A state field: host rows, device array, rows, values per row, and whether
+// the step is done writing it once nmd_correct is (see enqueue_step).
+struct StateField {
+    double *host;
+    double *dev;
+    int n, ncomp;
+    bool early;
+};
+
+int state_fields(des_ctx *c, const des_host_state *st, StateField *out)
+{
+    KP &p = c->kp;
+    const int nn = c->nn, ne = c->ne, nd = c->nd, npe = c->npe, nstr = c->nstr;
+    const size_t shp1 = (size_t)ne * npe;
+    const StateField all[] = {
+        {st->coord, p.x, nn, nd, false},
+        {st->coord0, p.x0, nn, nd, true},
+        {st->vel, p.v, nn, nd, false},
+        {st->force, p.f, nn, nd, false},
+        {st->temperature, p.T, nn, 1, true},
+        {st->mass, p.mass, nn, 1, false},
+        {st->tmass, p.tmass, nn, 1, false},
+        {st->volume_n, p.vol_n, nn, 1, false},
+        {st->ntmp, p.ntmp, nn, 1, true},
+        {st->volume, p.vol, ne, 1, false},
+        {st->volume_old, p.vol_old, ne, 1, false},
+        {st->stress, p.stress, ne, nstr, false},
+        {st->strain, p.strain, ne, nstr, false},
+        {st->strain_rate, p.srate, ne, nstr, true},
+        {st->plstrain, p.pls, ne, 1, true},
+        {st->delta_plstrain, p.dpls, ne, 1, true},
+        {st->stressyy, p.syy, ne, 1, true},
+        {st->dpressure, p.dp, ne, 1, true},
+        {st->edvoldt, p.edvoldt, ne, 1, true},
+        {st->shpdx, p.shp, ne, npe, false},
+        {nd == 3 ? st->shpdy : nullptr, p.shp + shp1, ne, npe, false},
+        {st->shpdz, p.shp + (size_t)(nd - 1) * shp1, ne, npe, false},
+    };
+    int k = 0;
+    for (const StateField &f : all)
+        if (f.host) out[k++] = f;
+    return k;
+}
+
+constexpr int MAX_STATE_FIELDS = 22;
+
+// download of every non-NULL field; with `early`, the fields the step's tail
+// does not write are copied once the step records ev_mid (the step must have
+// been launched from step_exec_mid), while the tail kernels still run
+int download_state(des_ctx *c, des_host_state *st, bool early)
+{
+    int rc;
+    if ((rc = ensure_xfer(c))) return rc;
+    StateField f[MAX_STATE_FIELDS];
+    const int nf = state_fields(c, st, f);
+    Pipe pp{c, false};
+    if (early) {
+        if ((rc = pp.begin(c->ev_mid))) return rc;
+        for (int k = 0; k < nf; ++k)
+            if (f[k].early && (rc = pp.field(f[k].host, f[k].dev, f[k].n, f[k].ncomp, true))) return rc;
+    }
+    if ((rc = pp.begin())) return rc;
+    for (int k = 0; k < nf; ++k)
+        if (!(early && f[k].early) && (rc = pp.field(f[k].host, f[k].dev, f[k].n, f[k].ncomp))) return rc;
+    if ((rc = pp.end())) return rc;
+    Clock ck;
+    CK(cudaMemcpyAsync(&ck, c->kp.clk, sizeof ck, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    st->time = ck.time;
+    st->dt = ck.dt;
+    st->steps = ck.steps;
+    return DES_OK;
+}
+
 }  // namespace
 
 int des_upload_state(des_ctx *c, const des_host_state *st)
@@ -531,34 +698,32 @@ int des_upload_state(des_ctx *c, const des_host_state *st)
     KP &p = c->kp;
     const int nn = c->nn, ne = c->ne, nd = c->nd, npe = c->npe, nstr = c->nstr;
     int rc;
-#define PUT(h, d, n, k)                                               \
-    do {                                                              \
-        if ((rc = put_field(c, (h), (d), (n), (k))) != DES_OK) return rc; \
-    } while (0)
+    if ((rc = ensure_xfer(c))) return rc;
+    // derived fields are taken from the host only when given as a set
+    des_host_state in = *st;
+    const bool have_shp = st->shpdx && st->shpdz && (nd == 2 || st->shpdy);
+    const bool have_mass = st->mass && st->tmass && st->volume_n;
+    if (!have_shp) in.shpdx = in.shpdy = in.shpdz = nullptr;
+    if (!have_mass) in.mass = in.tmass = in.volume_n = nullptr;
+    StateField f[MAX_STATE_FIELDS];
+    const int nf = state_fields(c, &in, f);
+    Pipe pp{c, true};
+    if ((rc = pp.begin())) return rc;
+    for (int k = 0; k < nf; ++k)
+        if ((rc = pp.field(f[k].host, f[k].dev, f[k].n, f[k].ncomp))) return rc;
 #define ZERO(d, bytes) CK(cudaMemsetAsync((d), 0, (bytes), c->stream))
-    PUT(st->coord, p.x, nn, nd);
-    if (st->coord0) PUT(st->coord0, p.x0, nn, nd);
-    else CK(cudaMemcpyAsync(p.x0, p.x, (size_t)nn * nd * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-    PUT(st->vel, p.v, nn, nd);
-    if (st->force) PUT(st->force, p.f, nn, nd);
-    else ZERO(p.f, (size_t)nn * nd * sizeof(double));
-    PUT(st->temperature, p.T, nn, 1);
-    PUT(st->volume_old, p.vol_old, ne, 1);
-    PUT(st->stress, p.stress, ne, nstr);
-    PUT(st->strain, p.strain, ne, nstr);
-    PUT(st->plstrain, p.pls, ne, 1);
-    if (st->strain_rate) PUT(st->strain_rate, p.srate, ne, nstr);
-    else ZERO(p.srate, (size_t)ne * nstr * sizeof(double));
-    if (st->delta_plstrain) PUT(st->delta_plstrain, p.dpls, ne, 1);
-    else ZERO(p.dpls, (size_t)ne * sizeof(double));
-    if (st->stressyy) PUT(st->stressyy, p.syy, ne, 1);
-    else ZERO(p.syy, (size_t)ne * sizeof(double));
-    if (st->dpressure) PUT(st->dpressure, p.dp, ne, 1);
-    else ZERO(p.dp, (size_t)ne * sizeof(double));
-    if (st->edvoldt) PUT(st->edvoldt, p.edvoldt, ne, 1);
-    else ZERO(p.edvoldt, (size_t)ne * sizeof(double));
-    if (st->ntmp) PUT(st->ntmp, p.ntmp, nn, 1);
-    else ZERO(p.ntmp, (size_t)nn * sizeof(double));
+    if (!st->force) ZERO(p.f, (size_t)nn * nd * sizeof(double));
+    if (!st->strain_rate) ZERO(p.srate, (size_t)ne * nstr * sizeof(double));
+    if (!st->delta_plstrain) ZERO(p.dpls, (size_t)ne * sizeof(double));
+    if (!st->stressyy) ZERO(p.syy, (size_t)ne * sizeof(double));
+    if (!st->dpressure) ZERO(p.dp, (size_t)ne * sizeof(double));
+    if (!st->edvoldt) ZERO(p.edvoldt, (size_t)ne * sizeof(double));
+    if (!st->ntmp) ZERO(p.ntmp, (size_t)nn * sizeof(double));
+#undef ZERO
+    if ((rc = pp.end())) return rc;
+    // what follows reads the uploaded fields
+    if (!st->coord0)
+        CK(cudaMemcpyAsync(p.x0, p.x, (size_t)nn * nd * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     {
         Clock ck{};
         ck.time = st->time;
@@ -569,22 +734,12 @@ int des_upload_state(des_ctx *c, const des_host_state *st)
         CK(cudaStreamSynchronize(c->stream));   // ck lives on this stack frame
     }
     KP q = p;   // per-function form
-    if (st->volume) PUT(st->volume, p.vol, ne, 1);
-    else if ((rc = check_launch(c, launch_geometry(q, c->stream, GEO_VOLUME)))) return rc;
-    if (st->shpdx && st->shpdz && (nd == 2 || st->shpdy)) {
-        PUT(st->shpdx, p.shp, ne, npe);
-        if (nd == 3) PUT(st->shpdy, p.shp + (size_t)ne * npe, ne, npe);
-        PUT(st->shpdz, p.shp + (size_t)(nd - 1) * ne * npe, ne, npe);
+    if (!st->volume && (rc = check_launch(c, launch_geometry(q, c->stream, GEO_VOLUME)))) return rc;
+    if (have_shp) {
         if (p.shp32 && (rc = check_launch(c, launch_f64_to_f32(p.shp, p.shp32, (long long)ne * npe * nd, c->stream))))
             return rc;
     } else if ((rc = check_launch(c, launch_geometry(q, c->stream, GEO_SHAPE)))) return rc;
-    if (st->mass && st->tmass && st->volume_n) {
-        PUT(st->mass, p.mass, nn, 1);
-        PUT(st->tmass, p.tmass, nn, 1);
-        PUT(st->volume_n, p.vol_n, nn, 1);
-    } else if ((rc = check_launch(c, launch_mass(q, c->stream)))) return rc;
-#undef PUT
-#undef ZERO
+    if (!have_mass && (rc = check_launch(c, launch_mass(q, c->stream)))) return rc;
     CK(cudaStreamSynchronize(c->stream));
     c->has_state = true;
     return DES_OK;
@@ -593,41 +748,7 @@ int des_upload_state(des_ctx *c, const des_host_state *st)
 int des_download_state(des_ctx *c, des_host_state *st)
 {
     if (!c || !st) return DES_EINPUT;
-    KP &p = c->kp;
-    const int nn = c->nn, ne = c->ne, nd = c->nd, npe = c->npe, nstr = c->nstr;
-    int rc;
-#define GET(h, d, n, k) \
-    if ((h) && (rc = get_field(c, (h), (d), (n), (k))) != DES_OK) return rc
-    GET(st->coord, p.x, nn, nd);
-    GET(st->coord0, p.x0, nn, nd);
-    GET(st->vel, p.v, nn, nd);
-    GET(st->force, p.f, nn, nd);
-    GET(st->temperature, p.T, nn, 1);
-    GET(st->mass, p.mass, nn, 1);
-    GET(st->tmass, p.tmass, nn, 1);
-    GET(st->volume_n, p.vol_n, nn, 1);
-    GET(st->ntmp, p.ntmp, nn, 1);
-    GET(st->volume, p.vol, ne, 1);
-    GET(st->volume_old, p.vol_old, ne, 1);
-    GET(st->stress, p.stress, ne, nstr);
-    GET(st->strain, p.strain, ne, nstr);
-    GET(st->strain_rate, p.srate, ne, nstr);
-    GET(st->plstrain, p.pls, ne, 1);
-    GET(st->delta_plstrain, p.dpls, ne, 1);
-    GET(st->stressyy, p.syy, ne, 1);
-    GET(st->dpressure, p.dp, ne, 1);
-    GET(st->edvoldt, p.edvoldt, ne, 1);
-    GET(st->shpdx, p.shp, ne, npe);
-    if (nd == 3) GET(st->shpdy, p.shp + (size_t)ne * npe, ne, npe);
-    GET(st->shpdz, p.shp + (size_t)(nd - 1) * ne * npe, ne, npe);
-#undef GET
-    Clock ck;
-    CK(cudaMemcpyAsync(&ck, p.clk, sizeof ck, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    st->time = ck.time;
-    st->dt = ck.dt;
-    st->steps = ck.steps;
-    return DES_OK;
+    return download_state(c, st, false);
 }
 
 namespace {
@@ -693,15 +814,16 @@ int transfer_fields(des_ctx *c, des_host_state *st, unsigned mask, bool up)
     if (!c || !st) return DES_EINPUT;
     if (mask & ~DES_F_ALL) return fail_msg(c->err, DES_EINPUT, "unknown field bits %#x", mask & ~DES_F_ALL);
     int rc;
+    if ((rc = ensure_xfer(c))) return rc;
+    Pipe pp{c, up};
+    if ((rc = pp.begin())) return rc;
     for (const FieldDesc &fd : kFields) {
         if (!(mask & fd.bit)) continue;
         double *h = st->*fd.member;
         if (!h) return fail_msg(c->err, DES_EINPUT, "field %#x selected but NULL", fd.bit);
         const int n = fd.node ? c->nn : c->ne;
         const int k = fd.ncomp == 0 ? c->nd : (fd.ncomp == -1 ? c->nstr : fd.ncomp);
-        double *d = device_field(c, fd.bit);
-        rc = up ? put_field(c, h, d, n, k) : get_field(c, h, d, n, k);
-        if (rc) return rc;
+        if ((rc = pp.field(h, device_field(c, fd.bit), n, k))) return rc;
     }
     if (mask & DES_F_SHP) {
         double *arr[3] = {st->shpdx, c->nd == 3 ? st->shpdy : nullptr, st->shpdz};
@@ -710,15 +832,15 @@ int transfer_fields(des_ctx *c, des_host_state *st, unsigned mask, bool up)
             if (a == 1 && c->nd == 2) continue;
             if (!arr[a]) return fail_msg(c->err, DES_EINPUT, "shape function array NULL");
             double *d = c->kp.shp + (size_t)slot * c->ne * c->npe;
-            rc = up ? put_field(c, arr[a], d, c->ne, c->npe) : get_field(c, arr[a], d, c->ne, c->npe);
-            if (rc) return rc;
+            if ((rc = pp.field(arr[a], d, c->ne, c->npe))) return rc;
             ++slot;
         }
-        if (up && c->kp.shp32) {   // keep the FP32 copy of the mixed step in step
-            rc = check_launch(c, launch_f64_to_f32(c->kp.shp, c->kp.shp32, (long long)c->ne * c->npe * c->nd,
-                                                   c->stream));
-            if (rc) return rc;
-        }
+    }
+    if ((rc = pp.end())) return rc;
+    if ((mask & DES_F_SHP) && up && c->kp.shp32) {   // keep the FP32 copy of the mixed step in step
+        rc = check_launch(c, launch_f64_to_f32(c->kp.shp, c->kp.shp32, (long long)c->ne * c->npe * c->nd,
+                                               c->stream));
+        if (rc) return rc;
     }
     if (mask & DES_F_CLOCK) {
         Clock ck;
@@ -868,7 +990,16 @@ namespace {
 
 bool use_mixed(const des_ctx *c) { return c->kp.shp32 != nullptr && !c->kp.mat.is_plane_strain; }
 
-int enqueue_step_mixed(des_ctx *c)
+// `mid` (optional) is recorded once nmd_correct is done: the kernels after it
+// (force and motion, geometry and rotation, mass sums, dt) write only x, v, f,
+// vol_old, vol, the shape functions, stress, strain, mass, tmass, volume_n
+// and the clock, so every other state field is final at that point.
+int record_mid(cudaEvent_t mid, cudaStream_t s)
+{
+    return mid ? (cudaEventRecordWithFlags(mid, s, cudaEventRecordExternal) == cudaSuccess ? 0 : -1) : 0;
+}
+
+int enqueue_step_mixed(des_ctx *c, cudaEvent_t mid)
 {
     const KP p = step_kp(c);
     cudaStream_t s = c->stream;
@@ -879,6 +1010,7 @@ int enqueue_step_mixed(des_ctx *c)
     n += launch_update_stress_mixed(p, s, true);
     n += launch_nmd_gather(p, s);
     n += launch_nmd_correct(p, s, true);
+    if (record_mid(mid, s)) return -1;
     n += launch_force(p, s, true);
     int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP | GEO_MASS_TERMS;
     if (p.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;   // FP32 increments in a mixed context
@@ -888,9 +1020,9 @@ int enqueue_step_mixed(des_ctx *c)
     return n;
 }
 
-int enqueue_step(des_ctx *c)
+int enqueue_step(des_ctx *c, cudaEvent_t mid)
 {
-    if (use_mixed(c)) return enqueue_step_mixed(c);
+    if (use_mixed(c)) return enqueue_step_mixed(c, mid);
     const KP p = step_kp(c);
     cudaStream_t s = c->stream;
     int n = 0;
@@ -905,6 +1037,7 @@ int enqueue_step(des_ctx *c)
     n += launch_update_stress(p, s, true);
     n += launch_nmd_gather(p, s);
     n += launch_nmd_correct(p, s, true);
+    if (record_mid(mid, s)) return -1;
     n += launch_force(p, s, true);
     int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP | GEO_MASS_TERMS;
     if (p.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;
@@ -914,17 +1047,24 @@ int enqueue_step(des_ctx *c)
     return n;
 }
 
-int build_step_graph(des_ctx *c)
+// One step as a CUDA graph; with `mid`, the graph also records it once
+// nmd_correct is done (step_exec_mid).
+int build_step_graph(des_ctx *c, cudaEvent_t mid = nullptr)
 {
     cudaGraph_t g;
+    cudaGraphExec_t &exec = mid ? c->step_exec_mid : c->step_exec;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    int n = enqueue_step(c);
+    int n = enqueue_step(c, mid);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&c->step_exec, g, 0);
+    if (n < 0) {
+        cudaGraphDestroy(g);
+        return fail_msg(c->err, DES_ECUDA, "step capture: recording the mid-step event failed");
+    }
+    e = cudaGraphInstantiate(&exec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) {
-        c->step_exec = nullptr;
+        exec = nullptr;
         return cuda_fail(c, e, "cudaGraphInstantiate");
     }
     c->step_kernels = n;
@@ -948,10 +1088,17 @@ int des_step(des_ctx *c, int nsteps)
 
 int des_step_host(des_ctx *c, des_host_state *st, int nsteps)
 {
+    if (!c || !st || nsteps < 0) return DES_EINPUT;
     int rc = des_upload_state(c, st);
     if (rc) return rc;
-    if ((rc = des_step(c, nsteps))) return rc;
-    return des_download_state(c, st);
+    if (nsteps == 0) return download_state(c, st, false);
+    // the last step comes from the graph that records ev_mid, so that the
+    // fields it no longer writes go back to the host while its tail runs
+    if ((rc = des_step(c, nsteps - 1))) return rc;
+    if (!c->step_exec_mid && (rc = build_step_graph(c, c->ev_mid))) return rc;
+    CK(cudaGraphLaunch(c->step_exec_mid, c->stream));
+    c->launches += c->step_kernels;
+    return download_state(c, st, true);
 }
 
 int des_synchronize(des_ctx *c)

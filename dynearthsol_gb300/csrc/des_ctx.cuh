@@ -12,6 +12,9 @@ namespace des {
 struct AdjWork;
 }
 
+// events of one pipelined transfer: start, done, one per multi-component field
+constexpr int DES_XFER_EVENTS = 32;
+
 struct des_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -28,6 +31,13 @@ struct des_ctx {
     unsigned long long *d_red = nullptr;
     double *d_ef[DES_EF_COUNT] = {};
     cudaGraphExec_t step_exec = nullptr;
+    // pipelined host transfers, created by the first state transfer
+    cudaStream_t xstream = nullptr;   // DMA between host rows and the device
+    cudaEvent_t xev[DES_XFER_EVENTS] = {};
+    double *d_xstage = nullptr;       // one AoS region per multi-component field
+    size_t xstage_doubles = 0;
+    cudaEvent_t ev_mid = nullptr;     // recorded by step_exec_mid once nmd_correct is done
+    cudaGraphExec_t step_exec_mid = nullptr;
     int step_kernels = 0;
     long long launches = 0;
     std::string err;
