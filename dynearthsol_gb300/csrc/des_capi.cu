@@ -938,16 +938,18 @@ PERFN(des_update_stress,
       n += ((p.shp32 && !p.mat.is_plane_strain) ? launch_update_stress_mixed(p, s, false)
                                                  : launch_update_stress(p, s, false)))
 PERFN(des_NMD_stress, n += launch_nmd_gather(p, s); n += launch_nmd_correct(p, s, false))
-PERFN(des_update_force, n += launch_facet_forces(p, s); n += launch_force(p, s, false))
-PERFN(des_update_velocity, n += launch_velocity(p, s))
+// in a mixed context, the fused-multiply-add forms of the mixed step
+PERFN(des_update_force,
+      n += launch_facet_forces(p, s); n += launch_force(p, s, false, p.shp32 && !p.mat.is_plane_strain))
+PERFN(des_update_velocity, n += launch_velocity(p, s, p.shp32 && !p.mat.is_plane_strain))
 PERFN(des_apply_vbcs, n += launch_vbcs(p, s))
-PERFN(des_update_coordinate, n += launch_coordinate(p, s))
+PERFN(des_update_coordinate, n += launch_coordinate(p, s, p.shp32 && !p.mat.is_plane_strain))
 PERFN(des_swap_volume, n += launch_geometry(p, s, GEO_COPY_OLD))
 PERFN(des_compute_volume, n += launch_geometry(p, s, GEO_VOLUME))
 PERFN(des_compute_mass, n += launch_mass(p, s))
 PERFN(des_compute_shape_fn, n += launch_geometry(p, s, GEO_SHAPE))
 PERFN(des_rotate_stress, n += launch_geometry(p, s, GEO_ROTATE))
-PERFN(des_update_mesh, n += launch_coordinate(p, s);
+PERFN(des_update_mesh, n += launch_coordinate(p, s, p.shp32 && !p.mat.is_plane_strain);
       n += launch_geometry(p, s, GEO_COPY_OLD | GEO_VOLUME); n += launch_mass(p, s);
       n += launch_geometry(p, s, GEO_SHAPE))
 
@@ -1011,7 +1013,7 @@ int enqueue_step_mixed(des_ctx *c, cudaEvent_t mid)
     n += launch_nmd_gather(p, s);
     n += launch_nmd_correct(p, s, true);
     if (record_mid(mid, s)) return -1;
-    n += launch_force(p, s, true);
+    n += launch_force(p, s, true, true);
     int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP | GEO_MASS_TERMS;
     if (p.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;   // FP32 increments in a mixed context
     n += launch_geometry(p, s, geo);

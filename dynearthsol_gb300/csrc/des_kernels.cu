@@ -338,7 +338,20 @@ __device__ __forceinline__ void damp(const KP &p, double &ff, double v)
     }
 }
 
-template <int ND>
+// a * b + c; with C, one fused multiply-add (the mixed step's kernels).
+// Without C it is the separately rounded product and sum of the FP64 step.
+template <bool C>
+__device__ __forceinline__ double madd(double a, double b, double c)
+{
+    return C ? fma(a, b, c) : a * b + c;
+}
+
+// CONTRACT: the mixed step's form, with the sums of products fused
+// (1 + 2 instead of 3 + 2 FP64 operations per component, and the update
+// f -= t * vol one fma), and dt f / m as dt f (1/m) with one recip_newton.
+// Rounding moves by an ulp of each force term, far below the FP32 strain
+// rate terms of the same step.
+template <int ND, bool CONTRACT = false>
 __global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
 {
     constexpr int NSTR = ND * (ND + 1) / 2;
@@ -363,14 +376,17 @@ __global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
             buoy = rho * gravity / NPE;
         }
         double sx = shp_at(p, 0, i, e), sz = shp_at(p, ND - 1, i, e);
+        // f -= (sum of products) * vol, written as madd(-t, vol, f): the same
+        // bits as the reference's expression when not contracted
         if (ND == 3) {
             double sy = shp_at(p, 1, i, e);
-            f[0] -= (s[0] * sx + s[3] * sy + s[4] * sz) * vol;
-            f[1] -= (s[3] * sx + s[1] * sy + s[5] * sz) * vol;
-            f[ND - 1] -= (s[4] * sx + s[5] * sy + s[2] * sz + buoy) * vol;
+            f[0] = madd<CONTRACT>(-madd<CONTRACT>(s[4], sz, madd<CONTRACT>(s[3], sy, s[0] * sx)), vol, f[0]);
+            f[1] = madd<CONTRACT>(-madd<CONTRACT>(s[5], sz, madd<CONTRACT>(s[1], sy, s[3] * sx)), vol, f[1]);
+            f[ND - 1] = madd<CONTRACT>(-(madd<CONTRACT>(s[2], sz, madd<CONTRACT>(s[5], sy, s[4] * sx)) + buoy), vol,
+                                       f[ND - 1]);
         } else {
-            f[0] -= (s[0] * sx + s[2] * sz) * vol;
-            f[ND - 1] -= (s[2] * sx + s[1] * sz + buoy) * vol;
+            f[0] = madd<CONTRACT>(-madd<CONTRACT>(s[2], sz, s[0] * sx), vol, f[0]);
+            f[ND - 1] = madd<CONTRACT>(-(madd<CONTRACT>(s[1], sz, s[2] * sx) + buoy), vol, f[ND - 1]);
         }
     }
     // gravity-induced stress BCs, in the reference's facet order
@@ -395,28 +411,36 @@ __global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
     if (!fused_motion) return;
     const double dt = p.clk->dt;
     const double m = p.mass[n];
+    if (CONTRACT) {
+        const double im = recip_newton(m);
 #pragma unroll
-    for (int d = 0; d < ND; ++d) v[d] += dt * f[d] / m;
+        for (int d = 0; d < ND; ++d) v[d] = fma(dt * f[d], im, v[d]);
+    } else {
+#pragma unroll
+        for (int d = 0; d < ND; ++d) v[d] += dt * f[d] / m;
+    }
     apply_vbcs_node<ND>(p, flag, v);
     bool bad = false;
 #pragma unroll
     for (int d = 0; d < ND; ++d) {
         const size_t o = (size_t)d * p.nn + n;
         p.v[o] = v[d];
-        double xn = p.x[o] + v[d] * dt;
+        double xn = madd<CONTRACT>(v[d], dt, p.x[o]);
         p.x[o] = xn;
         bad |= !isfinite(xn) || !isfinite(v[d]);
     }
     if (bad) set_err(p, DES_DEV_NONFINITE);
 }
 
-template <int ND>
+// CONTRACT: the form of k_force<ND, true>'s fused velocity update
+template <int ND, bool CONTRACT = false>
 __global__ void __launch_bounds__(TPB) k_velocity(KP p)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.nn * ND) return;
     int d = i / p.nn, n = i - d * p.nn;
-    p.v[i] += p.clk->dt * p.f[i] / p.mass[n];
+    if (CONTRACT) p.v[i] = fma(p.clk->dt * p.f[i], recip_newton(p.mass[n]), p.v[i]);
+    else p.v[i] += p.clk->dt * p.f[i] / p.mass[n];
     (void)d;
 }
 
@@ -434,12 +458,12 @@ __global__ void __launch_bounds__(TPB) k_vbcs(KP p)
     for (int d = 0; d < ND; ++d) p.v[(size_t)d * p.nn + n] = v[d];
 }
 
-template <int ND>
+template <int ND, bool CONTRACT = false>
 __global__ void __launch_bounds__(TPB) k_coordinate(KP p)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.nn * ND) return;
-    p.x[i] += p.v[i] * p.clk->dt;
+    p.x[i] = madd<CONTRACT>(p.v[i], p.clk->dt, p.x[i]);
 }
 
 // ==================================================================
@@ -963,15 +987,26 @@ int launch_facet_forces(const KP &p, cudaStream_t s)
     return 1;
 }
 
-int launch_force(const KP &p, cudaStream_t s, bool fused_motion)
+int launch_force(const KP &p, cudaStream_t s, bool fused_motion, bool contract)
 {
+    if (contract) {
+        if (p.nd == 3) k_force<3, true><<<nblocks(p.nn), TPB, 0, s>>>(p, (int)fused_motion);
+        else k_force<2, true><<<nblocks(p.nn), TPB, 0, s>>>(p, (int)fused_motion);
+        return 1;
+    }
     DISPATCH(k_force, nblocks(p.nn), p, (int)fused_motion);
     return 1;
 }
 
-int launch_velocity(const KP &p, cudaStream_t s)
+int launch_velocity(const KP &p, cudaStream_t s, bool contract)
 {
-    DISPATCH(k_velocity, nblocks((long long)p.nn * p.nd), p);
+    const int g = nblocks((long long)p.nn * p.nd);
+    if (contract) {
+        if (p.nd == 3) k_velocity<3, true><<<g, TPB, 0, s>>>(p);
+        else k_velocity<2, true><<<g, TPB, 0, s>>>(p);
+        return 1;
+    }
+    DISPATCH(k_velocity, g, p);
     return 1;
 }
 
@@ -981,9 +1016,15 @@ int launch_vbcs(const KP &p, cudaStream_t s)
     return 1;
 }
 
-int launch_coordinate(const KP &p, cudaStream_t s)
+int launch_coordinate(const KP &p, cudaStream_t s, bool contract)
 {
-    DISPATCH(k_coordinate, nblocks((long long)p.nn * p.nd), p);
+    const int g = nblocks((long long)p.nn * p.nd);
+    if (contract) {
+        if (p.nd == 3) k_coordinate<3, true><<<g, TPB, 0, s>>>(p);
+        else k_coordinate<2, true><<<g, TPB, 0, s>>>(p);
+        return 1;
+    }
+    DISPATCH(k_coordinate, g, p);
     return 1;
 }
 

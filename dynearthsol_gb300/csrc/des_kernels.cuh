@@ -29,10 +29,11 @@ int launch_update_stress(const KP &p, cudaStream_t s, bool fused);
 int launch_nmd_gather(const KP &p, cudaStream_t s);               // dp_nd -> ntmp
 int launch_nmd_correct(const KP &p, cudaStream_t s, bool with_facets);
 int launch_facet_forces(const KP &p, cudaStream_t s);
-int launch_force(const KP &p, cudaStream_t s, bool fused_motion);
-int launch_velocity(const KP &p, cudaStream_t s);
+// contract: the mixed step's fused multiply-add form (see k_force)
+int launch_force(const KP &p, cudaStream_t s, bool fused_motion, bool contract = false);
+int launch_velocity(const KP &p, cudaStream_t s, bool contract = false);
 int launch_vbcs(const KP &p, cudaStream_t s);
-int launch_coordinate(const KP &p, cudaStream_t s);
+int launch_coordinate(const KP &p, cudaStream_t s, bool contract = false);
 int launch_geometry(const KP &p, cudaStream_t s, int flags);
 int launch_mass(const KP &p, cudaStream_t s);
 // compute_mass from the element terms of a GEO_MASS_TERMS geometry pass (same sums, same order)
