@@ -470,6 +470,15 @@ __global__ void __launch_bounds__(TPB) k_coordinate(KP p)
 // element geometry: volume_old swap, compute_volume, compute_shape_fn,
 // rotate_stress, compute_dt element terms
 // ==================================================================
+// a * b - c * d; in the mixed step's form (C) with one fused multiply-add
+template <bool C>
+__device__ __forceinline__ double cof(double a, double b, double c, double d)
+{
+    return C ? fma(a, b, -(c * d)) : a * b - c * d;
+}
+
+// FAST_RECIP: the mixed step's form, 1/(6 vol) by recip_newton and the
+// cofactors with fused multiply-adds (an ulp from the FP64 step's values)
 template <int ND, bool FAST_RECIP = false>
 __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], double vol, double (*shp)[ND + 1])
 {
@@ -482,18 +491,18 @@ __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], double vol,
         double y12 = d1[1] - d2[1], y13 = d1[1] - d3[1], y23 = d2[1] - d3[1];
         double z01 = d0[2] - d1[2], z02 = d0[2] - d2[2], z03 = d0[2] - d3[2];
         double z12 = d1[2] - d2[2], z13 = d1[2] - d3[2], z23 = d2[2] - d3[2];
-        shp[0][0] = iv * (y13 * z12 - y12 * z13);
-        shp[0][1] = iv * (y02 * z23 - y23 * z02);
-        shp[0][2] = iv * (y13 * z03 - y03 * z13);
-        shp[0][3] = iv * (y01 * z02 - y02 * z01);
-        shp[1][0] = iv * (z13 * x12 - z12 * x13);
-        shp[1][1] = iv * (z02 * x23 - z23 * x02);
-        shp[1][2] = iv * (z13 * x03 - z03 * x13);
-        shp[1][3] = iv * (z01 * x02 - z02 * x01);
-        shp[ND - 1][0] = iv * (x13 * y12 - x12 * y13);
-        shp[ND - 1][1] = iv * (x02 * y23 - x23 * y02);
-        shp[ND - 1][2] = iv * (x13 * y03 - x03 * y13);
-        shp[ND - 1][3] = iv * (x01 * y02 - x02 * y01);
+        shp[0][0] = iv * cof<FAST_RECIP>(y13, z12, y12, z13);
+        shp[0][1] = iv * cof<FAST_RECIP>(y02, z23, y23, z02);
+        shp[0][2] = iv * cof<FAST_RECIP>(y13, z03, y03, z13);
+        shp[0][3] = iv * cof<FAST_RECIP>(y01, z02, y02, z01);
+        shp[1][0] = iv * cof<FAST_RECIP>(z13, x12, z12, x13);
+        shp[1][1] = iv * cof<FAST_RECIP>(z02, x23, z23, x02);
+        shp[1][2] = iv * cof<FAST_RECIP>(z13, x03, z03, x13);
+        shp[1][3] = iv * cof<FAST_RECIP>(z01, x02, z02, x01);
+        shp[ND - 1][0] = iv * cof<FAST_RECIP>(x13, y12, x12, y13);
+        shp[ND - 1][1] = iv * cof<FAST_RECIP>(x02, y23, x23, y02);
+        shp[ND - 1][2] = iv * cof<FAST_RECIP>(x13, y03, x03, y13);
+        shp[ND - 1][3] = iv * cof<FAST_RECIP>(x01, y02, x02, y01);
     } else {
         const double *d0 = d[0], *d1 = d[1], *d2 = d[2];
         double iv = FAST_RECIP ? recip_newton(2 * vol) : 1 / (2 * vol);

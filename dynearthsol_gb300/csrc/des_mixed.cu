@@ -227,7 +227,7 @@ __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, doubl
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const double *h = p.shp + (size_t)k * 4 * ne + e;   // dN_i/dx_k at h[i * ne]
-        out[k] = dd[0][k] * h[ne] + dd[1][k] * h[2 * ne] + dd[2][k] * h[3 * ne];
+        out[k] = fma(dd[2][k], h[3 * ne], fma(dd[1][k], h[2 * ne], dd[0][k] * h[ne]));
     }
     float s3 = 0, s4 = 0, s5 = 0;
 #pragma unroll
