@@ -152,12 +152,45 @@ __device__ __forceinline__ double divnd(double x)
     return x / ND;   // a power of two: the compiler multiplies by 0.5, exactly
 }
 
+// FP64 <-> FP32 conversions with integer instructions.  GB300 issues FP64
+// instructions at 1/64 of the FP32 rate, and the conversion instructions
+// occupy that same pipe: a conversion costs as much as an FP64 multiply.
+// These forms move the exponent and mantissa bits with a few integer
+// operations instead, which issue beside the FP64 work.
+//
+// f32_of(x): for |x| in [2^-126, 2^128), the nearest float, halfway cases
+// rounded away from zero (IEEE's ties-to-even differs only when x lies
+// exactly halfway between two floats); |x| < 2^-126 gives a signed zero;
+// |x| >= 2^128 gives +-inf, and NaN gives NaN.
+__device__ __forceinline__ float f32_of(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned mag = hi & 0x7fffffffu;
+    // exponent 1023 -> 127 bias, the top 23 mantissa bits, plus the next bit
+    // (a carry out of the mantissa correctly bumps the exponent)
+    unsigned u = (((mag - (896u << 20)) << 3) | (lo >> 29)) + ((lo >> 28) & 1u);
+    if (mag < (897u << 20)) u = 0;
+    if (mag >= (1151u << 20)) u = (mag > 0x7ff00000u || (mag == 0x7ff00000u && lo)) ? 0x7fc00000u : 0x7f800000u;
+    return __uint_as_float((hi & 0x80000000u) | u);
+}
+
+// f64_of(f): exact for every float but the subnormals, which give a signed
+// zero; +-inf and NaN stay +-inf and NaN.
+__device__ __forceinline__ double f64_of(float f)
+{
+    const unsigned u = __float_as_uint(f), mag = u & 0x7fffffffu;
+    unsigned hi = (mag >> 3) + ((mag >= 0x7f800000u ? 1792u : 896u) << 20);
+    unsigned lo = mag << 29;
+    if (mag < 0x00800000u) hi = lo = 0;
+    return __hiloint2double((int)((u & 0x80000000u) | hi), (int)lo);
+}
+
 // 1 / x from an FP32 seed and one FP64 Newton step (relative error ~1e-14,
 // for |x| within the FP32 normal range), for the mixed step only; the FP64
 // step divides
 __device__ __forceinline__ double recip_newton(double x)
 {
-    double r = (double)(1.0f / (float)x);
+    double r = f64_of(1.0f / f32_of(x));
     return r * (2.0 - x * r);
 }
 

@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
 #pragma unroll
                 for (int k = 0; k < ND; ++k)
 #pragma unroll
-                    for (int i = 0; i < NPE; ++i) p.shp32[((size_t)k * NPE + i) * ne + e] = (float)shp[k][i];
+                    for (int i = 0; i < NPE; ++i) p.shp32[((size_t)k * NPE + i) * ne + e] = f32_of(shp[k][i]);
             }
         } else if (flags & GEO_ROTATE) {
 #pragma unroll
@@ -610,13 +610,13 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
             for (int i = 1; i < NPE; ++i) {
                 double vi[ND];
                 load_node_v<ND>(p, nodes[i], vi);
-                const float d0 = (float)(vi[0] - v0[0]), d1 = (float)(vi[1] - v0[1]), d2 = (float)(vi[ND - 1] - v0[ND - 1]);
-                const float sx = (float)shp[0][i], sy = (float)shp[1][i], sz = (float)shp[ND - 1][i];
+                const float d0 = f32_of(vi[0] - v0[0]), d1 = f32_of(vi[1] - v0[1]), d2 = f32_of(vi[ND - 1] - v0[ND - 1]);
+                const float sx = f32_of(shp[0][i]), sy = f32_of(shp[1][i]), sz = f32_of(shp[ND - 1][i]);
                 w3 += 0.5f * (d0 * sy - d1 * sx);
                 w4 += 0.5f * (d0 * sz - d2 * sx);
                 w5 += 0.5f * (d1 * sz - d2 * sy);
             }
-            const float dtf = (float)p.clk->dt;
+            const float dtf = f32_of(p.clk->dt);
             double *arr[2] = {p.stress, p.strain};
 #pragma unroll
             for (int a = 0; a < 2; ++a) {
@@ -626,8 +626,8 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
                 // the isotropic part does not rotate: the normal-stress
                 // differences are taken in FP64, so the pressure never
                 // enters the FP32 products
-                const float d01 = (float)(S[0] - S[1]), d02 = (float)(S[0] - S[2]), d12 = (float)(S[1] - S[2]);
-                const float f3 = (float)S[3], f4 = (float)S[4], f5 = (float)S[5];
+                const float d01 = f32_of(S[0] - S[1]), d02 = f32_of(S[0] - S[2]), d12 = f32_of(S[1] - S[2]);
+                const float f3 = f32_of(S[3]), f4 = f32_of(S[4]), f5 = f32_of(S[5]);
                 float si[6];
                 si[0] = -2.0f * f3 * w3 - 2.0f * f4 * w4;
                 si[1] = 2.0f * f3 * w3 - 2.0f * f5 * w5;
@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
                 si[4] = d02 * w4 + f3 * w5 - f5 * w3;
                 si[5] = d12 * w5 + f3 * w4 + f4 * w3;
 #pragma unroll
-                for (int cc = 0; cc < 6; ++cc) arr[a][cc * ne + e] = S[cc] + (double)(dtf * si[cc]);
+                for (int cc = 0; cc < 6; ++cc) arr[a][cc * ne + e] = S[cc] + f64_of(dtf * si[cc]);
             }
         } else if (flags & GEO_ROTATE) {
             double v[NPE][ND];
@@ -1084,7 +1084,7 @@ int launch_quality(const KP &p, cudaStream_t s, unsigned long long *red)
 __global__ void k_f64_to_f32(const double *__restrict__ a, float *__restrict__ b, long long n)
 {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
+    if (i < n) b[i] = f32_of(a[i]);   // as the mixed geometry pass rounds them
 }
 
 int launch_f64_to_f32(const double *a, float *b, long long n, cudaStream_t s)

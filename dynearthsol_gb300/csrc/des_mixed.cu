@@ -48,29 +48,35 @@ static inline int nblocks_m(long long n)
 // ln(edot_II) = logf(mantissa) + exponent ln 2 (the FP32 log only sees
 // [0.5, 1)); 1/T from an FP32 seed and one FP64 Newton step; exp(ln visc) =
 // 2^k expf(r) with |r| <= ln2/2; the clamps to [visc_min, visc_max] are
-// exact.  The resulting viscosity is within ~2e-7 of the FP64 law.
+// exact.  The resulting viscosity is within ~2e-7 of the FP64 law.  Every
+// FP64 <-> FP32 conversion is f32_of / f64_of (integer instructions).
 __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *edot, double T)
 {
     if (p.mat.nmat != 1 || p.ef[DES_EF_LOG10_VISC]) return m_visc<3>(p, e, edot);
-    const double LN2 = 0.6931471805599453, INV_LN2 = 1.4426950408889634;
+    const double LN2 = 0.6931471805599453;
     float t[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) t[i] = (float)edot[i];
+    for (int i = 0; i < 6; ++i) t[i] = f32_of(edot[i]);
     const float a = (t[0] + t[1] + t[2]) * (1.0f / 3.0f);
     const float j2 = 0.5f * ((t[0] - a) * (t[0] - a) + (t[1] - a) * (t[1] - a) + (t[2] - a) * (t[2] - a))
         + t[3] * t[3] + t[4] * t[4] + t[5] * t[5];
     const float ed = fmaxf(sqrtf(j2), 1e-30f);
     int ex;
     const float mant = frexpf(ed, &ex);
-    const double ln_ed = (double)logf(mant) + (double)ex * LN2;
-    double r = (double)(1.0f / (float)T);
-    r = r * (2.0 - T * r);
-    const double lnv = p.mat.visc_lnc + p.mat.visc_pw[0] * ln_ed + p.mat.visc_qnr * r;
+    const double ln_ed = fma(f64_of((float)ex), LN2, f64_of(logf(mant)));
+    double r = f64_of(1.0f / f32_of(T));
+    r = r * fma(-T, r, 2.0);
+    const double lnv = fma(p.mat.visc_qnr, r, fma(p.mat.visc_pw[0], ln_ed, p.mat.visc_lnc));
     if (lnv <= p.mat.visc_lnmin) return p.mat.visc_min;
     if (lnv >= p.mat.visc_lnmax) return p.mat.visc_max;
-    const double k = rint(lnv * INV_LN2);
-    const float rr = (float)(lnv - k * LN2);
-    return ldexp((double)expf(rr), (int)k);
+    // exp(lnv) = 2^k exp(rr): any integer k near lnv / ln 2 keeps |rr| small,
+    // so k is rounded in FP32; rr = lnv - k ln 2 is one FP64 fma; 2^k goes
+    // into the exponent field of exp(rr) (in [0.7, 1.5], so the result stays
+    // normal for |k| <= 1000)
+    const float kf = fminf(fmaxf(rintf(f32_of(lnv) * 1.44269504f), -1000.0f), 1000.0f);
+    const float rr = f32_of(fma(-f64_of(kf), LN2, lnv));
+    const double m = f64_of(expf(rr));
+    return __hiloint2double(__double2hiint(m) + ((int)kf << 20), __double2loint(m));
 }
 
 // maxwell (rheology.cxx:118-134) with 1/viscosity and 1/(1+tmp) by
@@ -236,7 +242,7 @@ __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, doubl
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             dd[i - 1][d] = vi[d] - v0[d];
-            dv[i - 1][d] = (float)dd[i - 1][d];
+            dv[i - 1][d] = f32_of(dd[i - 1][d]);
         }
         sx[i - 1] = shp32_at(p, 0, i, e);
         sy[i - 1] = shp32_at(p, 1, i, e);
@@ -254,9 +260,9 @@ __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, doubl
         s4 += 0.5f * (dv[i][0] * sz[i] + dv[i][2] * sx[i]);
         s5 += 0.5f * (dv[i][1] * sz[i] + dv[i][2] * sy[i]);
     }
-    out[3] = (double)s3;
-    out[4] = (double)s4;
-    out[5] = (double)s5;
+    out[3] = f64_of(s3);
+    out[4] = f64_of(s4);
+    out[5] = f64_of(s5);
 #pragma unroll
     for (int c = 0; c < 6; ++c) p.srate[c * ne + e] = out[c];
 }
@@ -294,12 +300,12 @@ __global__ void __launch_bounds__(TPB_M) k_heat_dvoldt_mixed3(KP p, int heat, in
                 if (j == i) continue;
                 const float D = sxi * shp32_at(p, 0, j, e) + syi * shp32_at(p, 1, j, e)
                     + szi * shp32_at(p, 2, j, e);
-                diffusion += D * (float)(p.T[conn_at(p, j, e)] - Tn);
+                diffusion += D * f32_of(p.T[conn_at(p, j, e)] - Tn);
             }
-            const float volf = (float)vol;
-            const float kv = (float)(k_const ? p.mat.therm_cond[0] : m_k(p, e)) * volf;
-            const float rh = (float)((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * volf;
-            tdot += (double)(kv * diffusion - rh);
+            const float volf = f32_of(vol);
+            const float kv = f32_of(k_const ? p.mat.therm_cond[0] : m_k(p, e)) * volf;
+            const float rh = f32_of((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * volf;
+            tdot += f64_of(kv * diffusion - rh);
         }
         if (do_dvoldt) {
             const double dj = p.srate[e] + p.srate[(size_t)p.ne + e] + p.srate[2 * (size_t)p.ne + e];
@@ -345,7 +351,7 @@ __global__ void __launch_bounds__(TPB_M) k_elem_pass_mixed3(KP p, int heat)
         sy[i] = shp32_at(p, 1, i, e);
         sz[i] = shp32_at(p, 2, i, e);
     }
-    // D_ij = D_ji and (float)(T_i - T_j) = -(float)(T_j - T_i) bit for bit,
+    // D_ij = D_ji and f32_of(T_i - T_j) = -f32_of(T_j - T_i) bit for bit,
     // so each of the six products serves both rows
     float P[4][4];
 #pragma unroll
@@ -353,14 +359,14 @@ __global__ void __launch_bounds__(TPB_M) k_elem_pass_mixed3(KP p, int heat)
 #pragma unroll
         for (int j = i + 1; j < 4; ++j) {
             const float D = sx[i] * sx[j] + sy[i] * sy[j] + sz[i] * sz[j];
-            const float t = D * (float)(T[j] - T[i]);
+            const float t = D * f32_of(T[j] - T[i]);
             P[i][j] = t;
             P[j][i] = -t;
         }
     const bool k_const = (p.mat.nmat == 1) && !p.ef[DES_EF_THERM_COND];
-    const float volf = (float)vol;
-    const float kv = (float)(k_const ? p.mat.therm_cond[0] : m_k(p, e)) * volf;
-    const float rh = (float)((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * volf;
+    const float volf = f32_of(vol);
+    const float kv = f32_of(k_const ? p.mat.therm_cond[0] : m_k(p, e)) * volf;
+    const float rh = f32_of((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * volf;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         float diffusion = 0.0f;
@@ -380,7 +386,7 @@ __global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat)
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
         const int ent = p.sup_ent[q];
         const int e = ent >> 2, i = ent & 3;
-        if (heat) tdot += (double)p.hc[(size_t)i * ne + e];
+        if (heat) tdot += f64_of(p.hc[(size_t)i * ne + e]);
         dvoldt += p.qv[e];
     }
     p.ntmp[n] = dvoldt / p.vol_n[n];

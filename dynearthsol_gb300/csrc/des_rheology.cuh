@@ -350,7 +350,8 @@ __device__ __forceinline__ void jacobi3f(const float d[6], float w[3], float (&v
 // principal stresses of the full stress (principal_stresses3) carry errors
 // of a few eps64 (|m| + ||D||).  The screen passes an element only when both
 // yield functions clear the surface by tol = 2^-12 ||D||_F + 2^-40 |m|
-// (~4000 eps32 ||D||_F plus ~200 times the FP64 error in |m|), so a passed
+// (~4000 eps32 ||D||_F plus ~200 times the FP64 error in |m|), plus 2^-100
+// for the conversions' flush of magnitudes below 2^-126 to zero, so a passed
 // element is elastic in the FP64 test too: its output is its trial stress,
 // bit for bit, and the eigen-solve is skipped.  Every other element takes
 // the FP64 return map, including the choice of principal directions when
@@ -358,14 +359,14 @@ __device__ __forceinline__ void jacobi3f(const float d[6], float w[3], float (&v
 __device__ __forceinline__ bool clearly_elastic3(double amc, double anphi, double ten_max, const double *s)
 {
     const double m = (s[0] + s[1] + s[2]) * (1.0 / 3);
-    const float d[6] = {(float)(s[0] - m), (float)(s[1] - m), (float)(s[2] - m),
-                        (float)s[3], (float)s[4], (float)s[5]};
+    const float d[6] = {f32_of(s[0] - m), f32_of(s[1] - m), f32_of(s[2] - m),
+                        f32_of(s[3]), f32_of(s[4]), f32_of(s[5])};
     float w[3], v[3][3];
     jacobi3f(d, w, v);
     const float nf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
                            + 2.0f * (d[3] * d[3] + d[4] * d[4] + d[5] * d[5]));
-    const double tol = (double)nf * (1.0 / 4096) + 0x1p-40 * fabs(m);
-    const double p0 = m + (double)w[0], p2 = m + (double)w[2];
+    const double tol = f64_of(nf) * (1.0 / 4096) + 0x1p-40 * fabs(m) + 0x1p-100;
+    const double p0 = m + f64_of(w[0]), p2 = m + f64_of(w[2]);
     const double fs = p0 - p2 * anphi + amc;
     const double ft = p2 - ten_max;
     return fs > (1 + anphi) * tol && ft < -tol;
