@@ -61,6 +61,7 @@ KP step_kp(const des_ctx *c)
 {
     KP p = c->kp;
     p.rho_e = c->d_rho;
+    p.buoy_e = c->d_buoy;
     p.tdot = c->d_tdot;
     return p;
 }
@@ -311,6 +312,7 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
         add((void **)&d_qv, (size_t)ne * D);
     }
     add((void **)&c->d_rho, (size_t)ne * D);
+    add((void **)&c->d_buoy, (size_t)ne * D);
     add((void **)&p.me, (size_t)ne * D);
     add((void **)&p.tme, (size_t)ne * D);
     add((void **)&p.fv, (size_t)std::max(nbf, 1) * nd * D);
@@ -361,6 +363,7 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     p.fac_bdry = d_fb;
     p.emark = d_emark;
     p.rho_e = nullptr;
+    p.buoy_e = nullptr;
     p.tdot = p.ntmp;
     p.shp32 = d_shp32;
     p.hc = d_hc;

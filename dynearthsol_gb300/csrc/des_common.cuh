@@ -92,6 +92,7 @@ struct KP {
     // element fields
     double *stress, *strain, *srate, *pls, *dpls, *syy, *dp, *edvoldt, *vol, *vol_old, *shp;
     double *rho_e;                       // per-element density of the step (scratch), or null
+    double *buoy_e;                      // per-element rho g / NPE of the step (scratch), or null
     double *tdot;                        // node scratch for the heat gather (ntmp outside the fused step)
     double *fv;                          // [nd][nbf] per-facet stress-BC force (scratch)
     float *shp32;                        // FP32 copy of shp for the mixed step, or null
@@ -447,13 +448,37 @@ __device__ __forceinline__ double shp_at(const KP &p, int k, int i, int e)
 }
 
 // tetrahedron_volume (geometry.cxx:29-49)
+// the 18 coordinate differences of a tet that the volume and the shape
+// functions share (xij = x_i - x_j)
+struct TetEdges {
+    double x01, x02, x03, x12, x13, x23;
+    double y01, y02, y03, y12, y13, y23;
+    double z01, z02, z03, z12, z13, z23;
+};
+
+__device__ __forceinline__ TetEdges tet_edges(const double *d0, const double *d1, const double *d2,
+                                              const double *d3)
+{
+    TetEdges t;
+    t.x01 = d0[0] - d1[0], t.x02 = d0[0] - d2[0], t.x03 = d0[0] - d3[0];
+    t.x12 = d1[0] - d2[0], t.x13 = d1[0] - d3[0], t.x23 = d2[0] - d3[0];
+    t.y01 = d0[1] - d1[1], t.y02 = d0[1] - d2[1], t.y03 = d0[1] - d3[1];
+    t.y12 = d1[1] - d2[1], t.y13 = d1[1] - d3[1], t.y23 = d2[1] - d3[1];
+    t.z01 = d0[2] - d1[2], t.z02 = d0[2] - d2[2], t.z03 = d0[2] - d3[2];
+    t.z12 = d1[2] - d2[2], t.z13 = d1[2] - d3[2], t.z23 = d2[2] - d3[2];
+    return t;
+}
+
+__device__ __forceinline__ double tet_volume(const TetEdges &t)
+{
+    return div6(t.x01 * (t.y23 * t.z12 - t.y12 * t.z23) + t.x12 * (t.y01 * t.z23 - t.y23 * t.z01)
+                + t.x23 * (t.y12 * t.z01 - t.y01 * t.z12));
+}
+
 __device__ __forceinline__ double tet_volume(const double *d0, const double *d1, const double *d2,
                                              const double *d3)
 {
-    double x01 = d0[0] - d1[0], x12 = d1[0] - d2[0], x23 = d2[0] - d3[0];
-    double y01 = d0[1] - d1[1], y12 = d1[1] - d2[1], y23 = d2[1] - d3[1];
-    double z01 = d0[2] - d1[2], z12 = d1[2] - d2[2], z23 = d2[2] - d3[2];
-    return div6(x01 * (y23 * z12 - y12 * z23) + x12 * (y01 * z23 - y23 * z01) + x23 * (y12 * z01 - y01 * z12));
+    return tet_volume(tet_edges(d0, d1, d2, d3));
 }
 
 // triangle_area (geometry.cxx:53-83)

@@ -26,6 +26,7 @@ struct des_ctx {
     size_t pool_bytes = 0;
     double *d_tdot = nullptr;     // node scratch of the fused step
     double *d_rho = nullptr;      // element scratch of the fused step
+    double *d_buoy = nullptr;     // element scratch of the fused step: rho g / NPE
     double *d_stage = nullptr;    // AoS staging buffer
     size_t stage_doubles = 0;
     unsigned long long *d_red = nullptr;

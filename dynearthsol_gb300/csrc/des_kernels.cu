@@ -205,7 +205,12 @@ __global__ void __launch_bounds__(TPB) k_update_stress(KP p, int fused)
     p.pls[e] = pls;
     p.dpls[e] = dpls;
     p.dp[e] = dpr;
-    if (fused && p.rho_e) p.rho_e[e] = m_rho<ND>(p, e);   // temperature is final for this step
+    if (fused && p.rho_e) {   // temperature is final for this step
+        const double rho = m_rho<ND>(p, e);
+        p.rho_e[e] = rho;
+        // the force gather's buoyancy term, once per element instead of per node
+        if (p.buoy_e) p.buoy_e[e] = p.prm.gravity != 0 ? rho * p.prm.gravity / (ND + 1) : 0.0;
+    }
     if (bits) set_err(p, bits);
 }
 
@@ -371,7 +376,9 @@ __global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
         for (int c = 0; c < NSTR; ++c) s[c] = p.stress[c * ne + e];
         double vol = p.vol[e];
         double buoy = 0;
-        if (gravity != 0) {
+        if (p.buoy_e) {
+            buoy = p.buoy_e[e];
+        } else if (gravity != 0) {
             double rho = p.rho_e ? p.rho_e[e] : m_rho<ND>(p, e);
             buoy = rho * gravity / NPE;
         }
@@ -382,11 +389,13 @@ __global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
             double sy = shp_at(p, 1, i, e);
             f[0] = madd<CONTRACT>(-madd<CONTRACT>(s[4], sz, madd<CONTRACT>(s[3], sy, s[0] * sx)), vol, f[0]);
             f[1] = madd<CONTRACT>(-madd<CONTRACT>(s[5], sz, madd<CONTRACT>(s[1], sy, s[3] * sx)), vol, f[1]);
-            f[ND - 1] = madd<CONTRACT>(-(madd<CONTRACT>(s[2], sz, madd<CONTRACT>(s[5], sy, s[4] * sx)) + buoy), vol,
-                                       f[ND - 1]);
+            const double tz = CONTRACT ? fma(s[2], sz, fma(s[5], sy, fma(s[4], sx, buoy)))
+                                       : madd<false>(s[2], sz, madd<false>(s[5], sy, s[4] * sx)) + buoy;
+            f[ND - 1] = madd<CONTRACT>(-tz, vol, f[ND - 1]);
         } else {
             f[0] = madd<CONTRACT>(-madd<CONTRACT>(s[2], sz, s[0] * sx), vol, f[0]);
-            f[ND - 1] = madd<CONTRACT>(-(madd<CONTRACT>(s[1], sz, s[2] * sx) + buoy), vol, f[ND - 1]);
+            const double tz = CONTRACT ? fma(s[1], sz, fma(s[2], sx, buoy)) : madd<false>(s[1], sz, s[2] * sx) + buoy;
+            f[ND - 1] = madd<CONTRACT>(-tz, vol, f[ND - 1]);
         }
     }
     // gravity-induced stress BCs, in the reference's facet order
@@ -480,17 +489,14 @@ __device__ __forceinline__ double cof(double a, double b, double c, double d)
 // FAST_RECIP: the mixed step's form, 1/(6 vol) by recip_newton and the
 // cofactors with fused multiply-adds (an ulp from the FP64 step's values)
 template <int ND, bool FAST_RECIP = false>
-__device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], double vol, double (*shp)[ND + 1])
+__device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], const TetEdges &te, double vol,
+                                              double (*shp)[ND + 1])
 {
     if (ND == 3) {
-        const double *d0 = d[0], *d1 = d[1], *d2 = d[2], *d3 = d[3];
         double iv = FAST_RECIP ? recip_newton(6 * vol) : 1 / (6 * vol);
-        double x01 = d0[0] - d1[0], x02 = d0[0] - d2[0], x03 = d0[0] - d3[0];
-        double x12 = d1[0] - d2[0], x13 = d1[0] - d3[0], x23 = d2[0] - d3[0];
-        double y01 = d0[1] - d1[1], y02 = d0[1] - d2[1], y03 = d0[1] - d3[1];
-        double y12 = d1[1] - d2[1], y13 = d1[1] - d3[1], y23 = d2[1] - d3[1];
-        double z01 = d0[2] - d1[2], z02 = d0[2] - d2[2], z03 = d0[2] - d3[2];
-        double z12 = d1[2] - d2[2], z13 = d1[2] - d3[2], z23 = d2[2] - d3[2];
+        const double x01 = te.x01, x02 = te.x02, x03 = te.x03, x12 = te.x12, x13 = te.x13, x23 = te.x23;
+        const double y01 = te.y01, y02 = te.y02, y03 = te.y03, y12 = te.y12, y13 = te.y13, y23 = te.y23;
+        const double z01 = te.z01, z02 = te.z02, z03 = te.z03, z12 = te.z12, z13 = te.z13, z23 = te.z23;
         shp[0][0] = iv * cof<FAST_RECIP>(y13, z12, y12, z13);
         shp[0][1] = iv * cof<FAST_RECIP>(y02, z23, y23, z02);
         shp[0][2] = iv * cof<FAST_RECIP>(y13, z03, y03, z13);
@@ -571,9 +577,11 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
             load_node_x<ND>(p, nodes[i], c[i]);
         }
         double vol;
+        TetEdges te{};
+        if (ND == 3 && (flags & (GEO_VOLUME | GEO_SHAPE))) te = tet_edges(c[0], c[1], c[2], c[NPE - 1]);
         if (flags & GEO_COPY_OLD) p.vol_old[e] = p.vol[e];
         if (flags & GEO_VOLUME) {
-            if (ND == 3) vol = tet_volume(c[0], c[1], c[2], c[NPE - 1]);
+            if (ND == 3) vol = tet_volume(te);
             else vol = tri_area<2>(c[0], c[1], c[2]);
             p.vol[e] = vol;
             if (!(vol > 0)) set_err(p, DES_DEV_NEG_VOLUME);
@@ -582,8 +590,8 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
         }
         double shp[ND][NPE];
         if (flags & GEO_SHAPE) {
-            if (p.shp32) shape_fn_elem<ND, true>(c, vol, shp);
-            else shape_fn_elem<ND>(c, vol, shp);
+            if (p.shp32) shape_fn_elem<ND, true>(c, te, vol, shp);
+            else shape_fn_elem<ND>(c, te, vol, shp);
 #pragma unroll
             for (int k = 0; k < ND; ++k)
 #pragma unroll

@@ -176,9 +176,14 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
 #pragma unroll
         for (int i = 0; i < 6; ++i) sp[i] = s[i];
         elastic_mixed(bulkm, shearm, de, sp);
+        // mean and normal deviator of the trial stress, as second_invariant2_
+        // forms them: shared by the yield screen and, for a screened element,
+        // by J2 of the EVP choice
+        const double am = div3(sp[0] + sp[1] + sp[2]);
+        const double q[3] = {sp[0] - am, sp[1] - am, sp[2] - am};
         double depls = 0;
-        if (!clearly_elastic3(amc, anphi, ten_max, sp) &&
-            mc_return_<3>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp))
+        const bool screened = clearly_elastic3_dev(amc, anphi, ten_max, am, q, sp);
+        if (!screened && mc_return_<3>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp))
             bits |= DES_DEV_QL_NOCONV;
         if (rt == DES_RH_EP) {
 #pragma unroll
@@ -194,7 +199,10 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
             // viscosity (J2 of a small deviator formed from pressure-sized
             // components), and the two candidates differ in pressure (K dv
             // against K tr(de)): J2 is evaluated exactly as the FP64 step does
-            const double svII = second_invariant2_<3>(sv), spII = second_invariant2_<3>(sp);
+            const double svII = second_invariant2_<3>(sv);
+            const double spII = screened   // sp is the trial stress: second_invariant2_<3>(sp), bit for bit
+                ? 0.5 * (q[0] * q[0] + q[1] * q[1] + q[2] * q[2]) + sp[3] * sp[3] + sp[4] * sp[4] + sp[5] * sp[5]
+                : second_invariant2_<3>(sp);
             if (svII < spII) {
 #pragma unroll
                 for (int i = 0; i < 6; ++i) s[i] = sv[i];
@@ -215,7 +223,11 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
     p.pls[e] = pls;
     p.dpls[e] = dpls;
     p.dp[e] = (s[0] + s[1] + s[2]) - old_s;
-    if (fused && p.rho_e) p.rho_e[e] = m_rho_T(p, e, T);
+    if (fused && p.rho_e) {
+        const double rho = m_rho_T(p, e, T);
+        p.rho_e[e] = rho;
+        if (p.buoy_e) p.buoy_e[e] = p.prm.gravity != 0 ? rho * p.prm.gravity / 4 : 0.0;
+    }
     if (bits) set_err(p, bits);
 }
 

@@ -356,11 +356,12 @@ __device__ __forceinline__ void jacobi3f(const float d[6], float w[3], float (&v
 // bit for bit, and the eigen-solve is skipped.  Every other element takes
 // the FP64 return map, including the choice of principal directions when
 // two principal stresses (nearly) coincide, which FP32 cannot resolve.
-__device__ __forceinline__ bool clearly_elastic3(double amc, double anphi, double ten_max, const double *s)
+// The same screen given the mean stress m and the normal deviator q_i = s_i - m
+// (any FP64 rounding of m is covered by tol).
+__device__ __forceinline__ bool clearly_elastic3_dev(double amc, double anphi, double ten_max, double m,
+                                                     const double *q, const double *s)
 {
-    const double m = (s[0] + s[1] + s[2]) * (1.0 / 3);
-    const float d[6] = {f32_of(s[0] - m), f32_of(s[1] - m), f32_of(s[2] - m),
-                        f32_of(s[3]), f32_of(s[4]), f32_of(s[5])};
+    const float d[6] = {f32_of(q[0]), f32_of(q[1]), f32_of(q[2]), f32_of(s[3]), f32_of(s[4]), f32_of(s[5])};
     float w[3], v[3][3];
     jacobi3f(d, w, v);
     const float nf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
@@ -370,6 +371,13 @@ __device__ __forceinline__ bool clearly_elastic3(double amc, double anphi, doubl
     const double fs = p0 - p2 * anphi + amc;
     const double ft = p2 - ten_max;
     return fs > (1 + anphi) * tol && ft < -tol;
+}
+
+__device__ __forceinline__ bool clearly_elastic3(double amc, double anphi, double ten_max, const double *s)
+{
+    const double m = (s[0] + s[1] + s[2]) * (1.0 / 3);
+    const double q[3] = {s[0] - m, s[1] - m, s[2] - m};
+    return clearly_elastic3_dev(amc, anphi, ten_max, m, q, s);
 }
 
 // Mohr-Coulomb return map in principal space of the elastic trial stress s
