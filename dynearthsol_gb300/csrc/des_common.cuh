@@ -128,21 +128,31 @@ __device__ __forceinline__ double trace_(const double *s)
 // fractional part, in units of the quotient's last place, of 0, 1/3 or 2/3,
 // so it lies at least 1/6 ulp from every rounding midpoint, and the fma
 // rounds to the IEEE quotient: the result is bit-identical to x / 3.  Below
-// |x| = 2^-900, where x * YL could lose bits to underflow, it divides.
+// |x| = 2^-900, where x * YL could lose bits to underflow, it divides.  The
+// test |x| < 2^-900 reads the exponent field (biased exponent < 123) with
+// integer instructions, which keeps it off the FP64 pipe; it is true for the
+// same x, NaN included, as fabs(x) < 0x1p-900.
+__device__ __forceinline__ unsigned biased_exponent(double x)
+{
+    return ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
+}
+
 __device__ __forceinline__ double div3(double x)
 {
     constexpr double YH = 0x1.5555555555555p-2;    // RN(1/3)
     constexpr double YL = 0x1.5555555555555p-56;   // RN(1/3 - YH)
-    if (fabs(x) < 0x1p-900) return x / 3;
+    if (biased_exponent(x) < 123u) return x / 3;
     return fma(x, YH, x * YL);
 }
 
-// x / 6, bit-identical to the division: x * 0.5 is exact (x above the
-// subnormal range) and div3 rounds (x / 2) / 3 = x / 6 correctly
+// x / 6, bit-identical to the division: x / 2 is exact above the subnormal
+// range, taken as exponent - 1 on the bits for finite |x| >= 2^-900, and
+// div3 rounds (x / 2) / 3 = x / 6 correctly
 __device__ __forceinline__ double div6(double x)
 {
-    if (fabs(x) < 0x1p-900) return x / 6;
-    return div3(x * 0.5);
+    const unsigned e = biased_exponent(x);
+    if (e < 123u || e == 0x7ffu) return x / 6;
+    return div3(__hiloint2double(__double2hiint(x) - (1 << 20), __double2loint(x)));
 }
 
 // x / ND for ND = 2 or 3, bit-identical to the division
@@ -191,8 +201,8 @@ __device__ __forceinline__ double f64_of(float f)
 // step divides
 __device__ __forceinline__ double recip_newton(double x)
 {
-    double r = f64_of(1.0f / f32_of(x));
-    return r * (2.0 - x * r);
+    const double r = f64_of(1.0f / f32_of(x));
+    return fma(r, fma(-x, r, 1.0), r);   // r + r (1 - x r)
 }
 
 // utils.hpp:110-128
