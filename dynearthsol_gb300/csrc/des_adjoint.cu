@@ -560,7 +560,8 @@ __device__ __forceinline__ void maxwell_reverse(double K, double G, double visc,
                                                 const double *s, const double *go, double *gs, double *gde,
                                                 double &gG, double &gvisc, double &gdv)
 {
-    const double tmp = 0.5 * dt * G / visc;
+    const double ivisc = 1 / visc;
+    const double tmp = 0.5 * dt * G * ivisc;
     const double f1 = 1 - tmp, f2 = 1 / (1 + tmp);
     const double dev = div3(de[0] + de[1] + de[2]), s0 = div3(s[0] + s[1] + s[2]);
     double gf1 = 0, gf2 = 0, gs0 = 0, gdev = 0;
@@ -593,8 +594,8 @@ __device__ __forceinline__ void maxwell_reverse(double K, double G, double visc,
         gde[i] += gdev / 3;
     }
     const double gtmp = -gf1 - gf2 * f2 * f2;
-    gG += gtmp * 0.5 * dt / visc;
-    gvisc -= gtmp * tmp / visc;
+    gG += gtmp * 0.5 * dt * ivisc;
+    gvisc -= gtmp * tmp * ivisc;
 }
 
 // MatProps::visc for one material without markers, at an explicit mean
@@ -614,12 +615,11 @@ __device__ double visc_eval(const KP &p, int e, const double *edot, double T, do
     return dmin_(dmax_(raw, p.mat.visc_min), p.mat.visc_max);
 }
 
-// adjoint of the viscosity -> strain rate (corrected), mean temperature, log10 viscosity
-__device__ void visc_reverse(const KP &p, int e, const double *edot, double T, double gvisc, double *gedot,
-                             double &gT, double &glv)
+// adjoint of the viscosity -> strain rate (corrected), mean temperature, log10
+// viscosity; raw and ed are visc_eval's outputs for the same element
+__device__ void visc_reverse(const KP &p, int e, const double *edot, double T, double raw, double ed, double gvisc,
+                             double *gedot, double &gT, double &glv)
 {
-    double raw, ed;
-    visc_eval(p, e, edot, T, raw, ed);
     if (!(raw > p.mat.visc_min && raw < p.mat.visc_max)) return;   // clamped: no sensitivity
     if (p.ef[DES_EF_LOG10_VISC]) {
         glv += gvisc * raw * 2.302585092994046;   // d 10^x / dx = 10^x ln 10
@@ -645,6 +645,9 @@ __device__ void visc_reverse(const KP &p, int e, const double *edot, double T, d
 __device__ void plastic_props_reverse(const KP &p, int e, double pls, double gamc, double ganphi, double ganpsi,
                                       double ghardn, double gtmax, double *gpar, double &gpls)
 {
+    // an element whose return map was inactive passes zero adjoints: its
+    // contributions below are all zero, and the transcendentals are skipped
+    if (gamc == 0 && ganphi == 0 && ganpsi == 0 && ghardn == 0 && gtmax == 0) return;
     const double c0 = p.ef[DES_EF_COHESION0] ? p.ef[DES_EF_COHESION0][e] : p.mat.cohesion0[0];
     const double c1 = p.ef[DES_EF_COHESION1] ? p.ef[DES_EF_COHESION1][e] : p.mat.cohesion1[0];
     const double f0 = p.ef[DES_EF_FRICTION0] ? p.ef[DES_EF_FRICTION0][e] : p.mat.friction_angle0[0];
@@ -912,11 +915,12 @@ __global__ void __launch_bounds__(TPB_A) k_adj_stress(KP p, AdjBufs a, TapeStep 
             maxwell_reverse(K, G, visc, dt, de, s0, go, gs, gde, gG, gvisc, gdv);
         }
     }
-    if (viscous && gvisc != 0) visc_reverse(p, e, edot, T, gvisc, gec, gT, glv);
+    if (viscous && gvisc != 0) visc_reverse(p, e, edot, T, raw, ed, gvisc, gec, gT, glv);
 #pragma unroll
     for (int cc = 0; cc < 6; ++cc) gec[cc] += dt * gde[cc];
-    gvol += gdv / volo;
-    gvolo -= gdv * vol / (volo * volo);
+    const double ivo = 1 / volo;
+    gvol += gdv * ivo;
+    gvolo -= gdv * vol * ivo * ivo;
     // corrected strain rate -> strain rate before the correction, edvoldt
     const double tg = gec[0] + gec[1] + gec[2];
 #pragma unroll
