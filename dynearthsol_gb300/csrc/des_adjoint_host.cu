@@ -261,10 +261,12 @@ int adj_step(des_ctx *c, const TapeStep *t)
     if (t) CKA(cp(t->sss, p.stress, 6 * ne));
     n += launch_force(p, s, true);
     if (t) CKA(cp(t->f, p.f, 3 * nn));
-    int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE;
+    // mass from the geometry pass's element terms: the same sums, in the same
+    // order, as compute_mass's node gather (launch_mass), at a fifth of its cost
+    int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_MASS_TERMS;
     if (p.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;
     n += launch_geometry(p, s, geo);
-    n += launch_mass(p, s);
+    n += launch_mass_sum(p, s);
     return ctx_check_launch(c, n);
 }
 
