@@ -18,7 +18,10 @@ Metric: Mtet-steps/s = nelem x steps / time (higher is better).
            step (host<->device copies inside the timed region);
 * roofline: the dominant kernel (update_stress) timed alone with CUDA
            events: algorithmic bytes per launch / duration against the
-           measured HBM copy bandwidth (MEASURED_PEAKS.json);
+           measured HBM copy bandwidth (MEASURED_PEAKS.json); beside it,
+           fp64_pipe: its FP64 instructions per element (from the committed
+           ncu capture) per second against 2 per SM per clock, the roof that
+           binds on GB300;
 * cpu_baseline: the oracle (C restatement of the reference, OpenMP with the
            reference's two-colour band scatter) on this host's cores, on a
            bounded sample of the same workload.
@@ -67,15 +70,25 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic(kernel: str, workload: str):
-    """dram bytes per launch recorded from an ncu capture in profiles/."""
+def profile_value(kernel: str, workload: str, key: str):
+    """A per-launch figure recorded from an ncu capture in profiles/
+    ("key: value" line of the kernel's summary)."""
     p = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             return float(line.split(":", 1)[1].split()[0])
     return None
+
+
+def profile_traffic(kernel: str, workload: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/."""
+    return profile_value(kernel, workload, "traffic_bytes_per_launch")
+
+
+SM_COUNT = 152          # GB300
+FP64_PER_SM_CLK = 2     # FP64 thread instructions per SM per clock (ncu peak_sustained of DFMA)
 
 
 class ClockSampler:
@@ -369,6 +382,17 @@ def main():
                 "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                 "traffic": traffic, "kernel_ms": k_ms, "algorithmic_bytes_per_launch": alg,
                 "peak_kind": peak_kind}
+    # the roof that binds: FP64-pipe instructions per element (the committed
+    # ncu capture's count of FP64 add/mul/fma) over the kernel's live time,
+    # against 2 per SM per clock at the clock sampled during the timed steps
+    fp64_per_elem = profile_value(f"update_stress_{args.precision}", args.workload, "fp64_inst_per_elem")
+    if fp64_per_elem:
+        mhz = clocks["sm_mhz"] if clocks else 2070.0
+        ach = fp64_per_elem * ne / (k_ms / 1e3) / 1e9
+        peak = SM_COUNT * FP64_PER_SM_CLK * mhz / 1e3
+        roofline["fp64_pipe"] = {"instructions_per_elem": fp64_per_elem, "achieved_ginst_s": ach,
+                                 "peak_ginst_s": peak, "frac": ach / peak, "clock_mhz": mhz,
+                                 "clock": "sampled" if clocks else "nominal maximum"}
     step_alg = step_bytes_per_tet(nn, ne)
     step_gbs = step_alg * ne * args.steps / (ms / 1e3) / 1e9
 
