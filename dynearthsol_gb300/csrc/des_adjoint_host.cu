@@ -235,18 +235,14 @@ int adj_step(des_ctx *c, const TapeStep *t)
     };
     int n = 0;
     if (t) CKA(copy_state(tape_state(*t), live_state(c), nn, ne, s));
-    n += launch_strain_rate(p, s, true);
+    // strain rate, heat and dvoldt as the fused FP64 step forms them
+    const bool thermal = p.prm.has_thermal_diffusion != 0;
+    n += launch_elem_pass(p, s, thermal);
     if (t) CKA(cp(t->edot, p.srate, 6 * ne));
-    if (p.prm.has_thermal_diffusion) {
-        n += launch_heat_and_dvoldt(p, s);
-        if (t) {
-            CKA(cp(t->tdot, p.tdot, nn));
-            CKA(cp(t->ntmp, p.ntmp, nn));
-        }
-        n += launch_temperature_update(p, s);
-    } else {
-        n += launch_dvoldt(p, s);
-        if (t) CKA(cp(t->ntmp, p.ntmp, nn));
+    n += launch_node_pass(p, s, thermal);
+    if (t) {
+        if (thermal) CKA(cp(t->tdot, p.tdot, nn));
+        CKA(cp(t->ntmp, p.ntmp, nn));
     }
     n += launch_update_stress(p, s, true);
     if (t) {

@@ -305,11 +305,13 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     add((void **)&p.shp, (size_t)ne * npe * nd * D);
     const bool mixed3 = (precision == DES_PREC_MIXED) && nd == 3;
     float *d_shp32 = nullptr, *d_hc = nullptr;
-    double *d_qv = nullptr;
+    double *d_qv = nullptr, *d_hc64 = nullptr;
+    add((void **)&d_qv, (size_t)ne * D);
     if (mixed3) {
         add((void **)&d_shp32, (size_t)ne * npe * nd * sizeof(float));
         add((void **)&d_hc, (size_t)ne * npe * sizeof(float));
-        add((void **)&d_qv, (size_t)ne * D);
+    } else {
+        add((void **)&d_hc64, (size_t)ne * npe * D);
     }
     add((void **)&c->d_rho, (size_t)ne * D);
     add((void **)&c->d_buoy, (size_t)ne * D);
@@ -368,6 +370,7 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     p.shp32 = d_shp32;
     p.hc = d_hc;
     p.qv = d_qv;
+    p.hc64 = d_hc64;
     for (int i = 0; i < DES_NBDRYTYPES; ++i)
         for (int d = 0; d < 3; ++d) {
             p.bnormals[i][d] = mesh->bnormals[i][d];
@@ -1032,13 +1035,8 @@ int enqueue_step(des_ctx *c, cudaEvent_t mid)
     cudaStream_t s = c->stream;
     int n = 0;
     const bool thermal = p.prm.has_thermal_diffusion != 0;
-    n += launch_strain_rate(p, s, true);
-    if (thermal) {
-        n += launch_heat_and_dvoldt(p, s);
-        n += launch_temperature_update(p, s);
-    } else {
-        n += launch_dvoldt(p, s);
-    }
+    n += launch_elem_pass(p, s, thermal);   // strain rate, element dvoldt and heat terms
+    n += launch_node_pass(p, s, thermal);   // nodal sums, temperature update
     n += launch_update_stress(p, s, true);
     n += launch_nmd_gather(p, s);
     n += launch_nmd_correct(p, s, true);

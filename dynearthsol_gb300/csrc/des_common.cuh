@@ -97,7 +97,8 @@ struct KP {
     double *fv;                          // [nd][nbf] per-facet stress-BC force (scratch)
     float *shp32;                        // FP32 copy of shp for the mixed step, or null
     float *hc;                           // [4][ne] per-element heat terms of the mixed step, or null
-    double *qv;                          // [ne] per-element dvoldt term of the mixed step, or null
+    double *qv;                          // [ne] per-element dvoldt term of the fused steps, or null
+    double *hc64;                        // [NPE][ne] per-element heat terms of the FP64 step, or null
     double *me, *tme;                    // [ne] per-element mass and tmass terms of the fused step
     const double *ef[DES_EF_COUNT];      // per-element overrides or null
     Clock *clk;

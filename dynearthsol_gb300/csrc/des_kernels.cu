@@ -141,6 +141,88 @@ __global__ void __launch_bounds__(TPB) k_node_gather1(KP p)
     if (DVOLDT) p.ntmp[n] = dvoldt / p.vol_n[n];
 }
 
+// The fused step's form of the same three functions (update_strain_rate,
+// the heat gather of update_temperature, compute_dvoldt), element-centric.
+// k_elem_pass writes the strain rate, the element's dvoldt term qv = tr(edot)
+// vol and, with heat, its contribution to each of its nodes' tdot (slot i of
+// hc64).  The stencil D_ij = dN_i . dN_j is formed once per element: D_ji is
+// the same products in the same order, so every slot holds the very value
+// heat_term gives for (e, i), at 10 instead of 16 dot products.
+// k_node_pass sums the slots and the qv over each node's support in
+// ascending element order -- the node-centric kernels' order -- and applies
+// the temperature update.  The bits are those of k_strain_rate,
+// k_node_gather1 and k_temperature_update.
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_elem_pass(KP p, int heat)
+{
+    constexpr int NPE = ND + 1, NSTR = ND * (ND + 1) / 2;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e == 0) {   // var.steps++; var.time += var.dt (dynearthsol.cxx:325-326)
+        p.clk->steps += 1;
+        p.clk->time += p.clk->dt;
+    }
+    if (e >= p.ne) return;
+    const size_t ne = p.ne;
+    double sr[NSTR];
+    strain_rate_elem<ND>(p, e, sr);
+#pragma unroll
+    for (int c = 0; c < NSTR; ++c) p.srate[(size_t)c * ne + e] = sr[c];
+    const double vol = p.vol[e];
+    double dj;
+    if (ND == 3) dj = sr[0] + sr[1] + sr[2];
+    else dj = sr[0] + sr[1];
+    p.qv[e] = dj * vol;
+    if (!heat) return;
+    const double kv = m_k(p, e) * vol;
+    const double rh = ((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * vol;
+    double sx[NPE], sy[NPE], sz[NPE], T[NPE];
+#pragma unroll
+    for (int i = 0; i < NPE; ++i) {
+        sx[i] = shp_at(p, 0, i, e);
+        sy[i] = (ND == 3) ? shp_at(p, 1, i, e) : 0.0;
+        sz[i] = shp_at(p, ND - 1, i, e);
+        T[i] = p.T[conn_at(p, i, e)];
+    }
+    double D[NPE][NPE];
+#pragma unroll
+    for (int i = 0; i < NPE; ++i)
+#pragma unroll
+        for (int j = i; j < NPE; ++j) {
+            D[i][j] = (ND == 3) ? (sx[i] * sx[j] + sy[i] * sy[j] + sz[i] * sz[j]) : (sx[i] * sx[j] + sz[i] * sz[j]);
+            D[j][i] = D[i][j];
+        }
+#pragma unroll
+    for (int i = 0; i < NPE; ++i) {
+        double diffusion = 0;
+#pragma unroll
+        for (int j = 0; j < NPE; ++j) diffusion += D[i][j] * T[j];
+        p.hc64[(size_t)i * ne + e] = diffusion * kv - rh;
+    }
+}
+
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_node_pass(KP p, int heat)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.nn) return;
+    const size_t ne = p.ne;
+    double tdot = 0, dvoldt = 0;
+    for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+        const int ent = p.sup_ent[q];
+        const int e = ent >> 2, i = ent & 3;
+        if (heat) tdot += p.hc64[(size_t)i * ne + e];
+        dvoldt += p.qv[e];
+    }
+    p.ntmp[n] = dvoldt / p.vol_n[n];
+    if (heat) {   // temperature update + Dirichlet BC (fields.cxx:151-162)
+        p.tdot[n] = tdot;
+        const unsigned flag = p.bcflag[n];
+        if (flag & BOUNDZ1) p.T[n] = p.prm.surface_temperature;
+        else if ((flag & BOUNDZ0) && !p.prm.has_fixed_bottom_temperature) p.T[n] = p.prm.mantle_temperature;
+        else p.T[n] -= tdot * p.clk->dt / p.tmass[n];
+    }
+}
+
 // temperature update + Dirichlet BC (fields.cxx:151-162)
 __global__ void __launch_bounds__(TPB) k_temperature_update(KP p)
 {
@@ -956,6 +1038,18 @@ int launch_dvoldt(const KP &p, cudaStream_t s)
 {
     if (p.nd == 3) k_node_gather1<3, false, true><<<nblocks(p.nn), TPB, 0, s>>>(p);
     else k_node_gather1<2, false, true><<<nblocks(p.nn), TPB, 0, s>>>(p);
+    return 1;
+}
+
+int launch_elem_pass(const KP &p, cudaStream_t s, bool heat)
+{
+    DISPATCH(k_elem_pass, nblocks(p.ne), p, (int)heat);
+    return 1;
+}
+
+int launch_node_pass(const KP &p, cudaStream_t s, bool heat)
+{
+    DISPATCH(k_node_pass, nblocks(p.nn), p, (int)heat);
     return 1;
 }
 

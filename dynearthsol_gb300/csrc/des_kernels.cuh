@@ -24,6 +24,11 @@ int launch_heat_gather(const KP &p, cudaStream_t s);              // tdot -> p.t
 int launch_temperature_update(const KP &p, cudaStream_t s);       // T from p.tdot
 int launch_dvoldt(const KP &p, cudaStream_t s);                   // -> ntmp
 int launch_heat_and_dvoldt(const KP &p, cudaStream_t s);          // fused: tdot -> p.tdot, dvoldt -> ntmp
+// the FP64 step's element-centric form of strain rate + heat gather + dvoldt
+// (+ clock advance) and of the node sums + temperature update: the same bits
+// (needs p.qv and, with heat, p.hc64)
+int launch_elem_pass(const KP &p, cudaStream_t s, bool heat);
+int launch_node_pass(const KP &p, cudaStream_t s, bool heat);
 int launch_edvoldt(const KP &p, cudaStream_t s);
 int launch_update_stress(const KP &p, cudaStream_t s, bool fused);
 int launch_nmd_gather(const KP &p, cudaStream_t s);               // dp_nd -> ntmp
