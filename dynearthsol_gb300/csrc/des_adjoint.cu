@@ -616,7 +616,8 @@ __device__ double visc_eval(const KP &p, int e, const double *edot, double T, do
 }
 
 // adjoint of the viscosity -> strain rate (corrected), mean temperature, log10
-// viscosity; raw and ed are visc_eval's outputs for the same element
+// viscosity; raw is the unclamped viscosity and ed the strain-rate invariant
+// of visc_eval for the same element (ed < 0: not known yet)
 __device__ void visc_reverse(const KP &p, int e, const double *edot, double T, double raw, double ed, double gvisc,
                              double *gedot, double &gT, double &glv)
 {
@@ -628,6 +629,7 @@ __device__ void visc_reverse(const KP &p, int e, const double *edot, double T, d
     const double gas_constant = 8.3144;
     const double q = p.mat.visc_activation_energy[0] / (p.mat.visc_exponent[0] * gas_constant);
     gT += gvisc * raw * (-q / (T * T));
+    if (ed < 0) ed = dmax_(second_invariant_<3>(edot), 1e-30);   // as visc_eval forms it
     if (ed > 1e-30) {
         const double ged = gvisc * raw * p.mat.visc_pw[0] / ed;
         const double gj2 = ged / (2 * ed);
@@ -876,9 +878,14 @@ __global__ void __launch_bounds__(TPB_A) k_adj_stress(KP p, AdjBufs a, TapeStep 
     double gG = 0, gvisc = 0, gdv = 0, gT = 0, glv = 0, gpls_props = 0;
     double gpar[DES_EF_COUNT] = {};
     const int rt = p.mat.rheol_type;
-    double visc = 0, raw, ed;
+    // the viscosity and the EVP branch: the forward recompute's, from the
+    // tape (else evaluated again, as the forward does)
+    double visc = 0, raw = 0, ed = -1;
     const bool viscous = (rt & DES_RH_VISCOUS) != 0;
-    if (viscous) visc = visc_eval(p, e, edot, T, raw, ed);
+    if (viscous) {
+        if (t.visc) raw = visc = t.visc[e];   // unclamped: raw == visc; clamped: no sensitivity either way
+        else visc = visc_eval(p, e, edot, T, raw, ed);
+    }
     if (rt == DES_RH_ELASTIC) {
         elastic_reverse(K, G, de, go, gs, gde, gG);
     } else if (rt == DES_RH_MAXWELL) {
@@ -886,25 +893,28 @@ __global__ void __launch_bounds__(TPB_A) k_adj_stress(KP p, AdjBufs a, TapeStep 
     } else {   // EP or EVP
         double amc, anphi, anpsi, hardn, tmax;
         m_plastic_props(p, e, pls, amc, anphi, anpsi, hardn, tmax);
-        double S[6];
-#pragma unroll
-        for (int cc = 0; cc < 6; ++cc) S[cc] = s0[cc];
-        elastic_<3>(K, G, de, S);
         bool plastic = true;
         if (rt == DES_RH_EVP) {
-            const double dv = vol / volo - 1;
-            double sv[6], sp[6];
+            if (t.evp) {
+                plastic = t.evp[e] != 0;
+            } else {
+                const double dv = vol / volo - 1;
+                double sv[6], sp[6];
 #pragma unroll
-            for (int cc = 0; cc < 6; ++cc) {
-                sv[cc] = s0[cc];
-                sp[cc] = S[cc];
+                for (int cc = 0; cc < 6; ++cc) sv[cc] = sp[cc] = s0[cc];
+                elastic_<3>(K, G, de, sp);
+                maxwell_<3>(K, G, visc, dt, dv, de, sv);
+                double depls;
+                if (!clearly_elastic3(amc, anphi, tmax, sp))
+                    mc_return_<3>(K, G, amc, anphi, anpsi, hardn, tmax, depls, sp);
+                plastic = !(second_invariant2_<3>(sv) < second_invariant2_<3>(sp));
             }
-            maxwell_<3>(K, G, visc, dt, dv, de, sv);
-            double depls;
-            if (!clearly_elastic3(amc, anphi, tmax, sp)) mc_return_<3>(K, G, amc, anphi, anpsi, hardn, tmax, depls, sp);
-            plastic = !(second_invariant2_<3>(sv) < second_invariant2_<3>(sp));
         }
         if (plastic) {
+            double S[6];   // the elastic trial stress
+#pragma unroll
+            for (int cc = 0; cc < 6; ++cc) S[cc] = s0[cc];
+            elastic_<3>(K, G, de, S);
             double gS[6] = {0, 0, 0, 0, 0, 0};
             double gamc = 0, ganphi = 0, ganpsi = 0, ghardn = 0, gtmax = 0;
             mc_return_reverse(K, G, amc, anphi, anpsi, hardn, tmax, S, go, a.apls[e], gS, gG, gamc, ganphi, ganpsi,

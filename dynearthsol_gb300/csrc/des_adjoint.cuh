@@ -32,6 +32,8 @@ struct TapeStep {
     double *dpn;     // [nn] NMD nodal pressure change
     double *sss;     // [6][ne] stress after NMD_stress (before the rotation)
     double *f;       // [3][nn] force after damping
+    double *visc;    // [ne] viscosity the rheology used (Maxwell, EVP)
+    unsigned char *evp;   // [ne] EVP branch taken: 1 elasto-plastic, 0 Maxwell
 };
 
 // adjoint buffers; "_k" fields hold the adjoint of the state at the start

@@ -212,6 +212,8 @@ int alloc_tape(des_ctx *c, AdjWork *w, int cap)
         cv2.add((void **)&t.dpn, nn * D);
         cv2.add((void **)&t.sss, 6 * ne * D);
         cv2.add((void **)&t.f, 3 * nn * D);
+        cv2.add((void **)&t.visc, ne * D);
+        cv2.add((void **)&t.evp, ne);
     }
     cudaError_t e = cudaMalloc((void **)&w->tape_mem, cv2.total());
     if (e != cudaSuccess)
@@ -227,7 +229,11 @@ int alloc_tape(des_ctx *c, AdjWork *w, int cap)
 // kernels read are copied into it
 int adj_step(des_ctx *c, const TapeStep *t)
 {
-    const KP p = ctx_step_kp(c);
+    KP p = ctx_step_kp(c);
+    if (t) {   // the rheology writes the viscosity and the EVP branch it took
+        p.tape_visc = t->visc;
+        p.tape_evp = t->evp;
+    }
     cudaStream_t s = c->stream;
     const size_t nn = c->nn, ne = c->ne, D = sizeof(double);
     auto cp = [&](double *dst, const double *src, size_t n) {

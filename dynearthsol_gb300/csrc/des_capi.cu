@@ -371,6 +371,8 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     p.hc = d_hc;
     p.qv = d_qv;
     p.hc64 = d_hc64;
+    p.tape_visc = nullptr;
+    p.tape_evp = nullptr;
     for (int i = 0; i < DES_NBDRYTYPES; ++i)
         for (int d = 0; d < 3; ++d) {
             p.bnormals[i][d] = mesh->bnormals[i][d];

@@ -99,6 +99,10 @@ struct KP {
     float *hc;                           // [4][ne] per-element heat terms of the mixed step, or null
     double *qv;                          // [ne] per-element dvoldt term of the fused steps, or null
     double *hc64;                        // [NPE][ne] per-element heat terms of the FP64 step, or null
+    // set only by the reverse mode's forward recompute: the viscosity the
+    // rheology used and the EVP branch it took (1: elasto-plastic), per element
+    double *tape_visc;
+    unsigned char *tape_evp;
     double *me, *tme;                    // [ne] per-element mass and tmass terms of the fused step
     const double *ef[DES_EF_COUNT];      // per-element overrides or null
     Clock *clk;

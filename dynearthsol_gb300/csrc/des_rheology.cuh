@@ -570,7 +570,9 @@ __device__ unsigned update_stress_elem(const KP &p, int e, double dt, double *s,
         viscous_<ND>(m_bulkm(p, e), m_visc<ND>(p, e, edot), trace_<ND>(es), edot, s);
     } else if (rt == DES_RH_MAXWELL) {
         double dv = vol / vol_old - 1;
-        maxwell_<ND>(m_bulkm(p, e), m_shearm(p, e), m_visc<ND>(p, e, edot), dt, dv, de, s);
+        const double viscosity = m_visc<ND>(p, e, edot);
+        if (p.tape_visc) p.tape_visc[e] = viscosity;
+        maxwell_<ND>(m_bulkm(p, e), m_shearm(p, e), viscosity, dt, dv, de, s);
     } else if (rt == DES_RH_EP) {
         double depls = 0, amc, anphi, anpsi, hardn, ten_max;
         double bulkm = m_bulkm(p, e), shearm = m_shearm(p, e);
@@ -585,6 +587,7 @@ __device__ unsigned update_stress_elem(const KP &p, int e, double dt, double *s,
         double depls = 0;
         double bulkm = m_bulkm(p, e), shearm = m_shearm(p, e);
         double viscosity = m_visc<ND>(p, e, edot);
+        if (p.tape_visc) p.tape_visc[e] = viscosity;
         double dv = vol / vol_old - 1;
         double sv[NSTR];
 #pragma unroll
@@ -601,6 +604,7 @@ __device__ unsigned update_stress_elem(const KP &p, int e, double dt, double *s,
         else if (elasto_plastic_<ND>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, sp))
             bits |= DES_DEV_QL_NOCONV;
         double spII = second_invariant2_<ND>(sp);
+        if (p.tape_evp) p.tape_evp[e] = svII < spII ? 0 : 1;
         if (svII < spII) {
 #pragma unroll
             for (int i = 0; i < NSTR; ++i) s[i] = sv[i];
