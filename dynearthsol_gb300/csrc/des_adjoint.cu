@@ -1034,24 +1034,46 @@ __global__ void __launch_bounds__(TPB_A) k_adj_kinematics(KP p, AdjBufs a, TapeS
         }
         const double k = m_k(p, e), kv = k * vol, hrcp = p.mat.hr_over_cp;
         double gkv = 0, grh = 0;
+        // tdot_i = kv sum_j D_ij T_j - rh with the symmetric D_ij = dN_i . dN_j:
+        // D is formed once (10 entries), and the adjoints of D_ij and D_ji,
+        // kg_i T_j and kg_j T_i (kg = kv gtd), are folded into one symmetric
+        // H_mk, so that d/d dN_m = sum_k H_mk dN_k
+        double D[4][4], kg[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            kg[i] = kv * gtd[i];
+#pragma unroll
+            for (int j = i; j < 4; ++j) {
+                D[i][j] = sh[0][i] * sh[0][j] + sh[1][i] * sh[1][j] + sh[2][i] * sh[2][j];
+                D[j][i] = D[i][j];
+            }
+        }
+        double H[4][4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             double diffusion = 0;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const double D = sh[0][i] * sh[0][j] + sh[1][i] * sh[1][j] + sh[2][i] * sh[2][j];
-                diffusion += D * Tn[j];
-                gTn[j] += kv * gtd[i] * D;
-                const double gD = kv * gtd[i] * Tn[j];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    gsh[c][i] += gD * sh[c][j];
-                    gsh[c][j] += gD * sh[c][i];
-                }
+                diffusion += D[i][j] * Tn[j];
+                gTn[i] += D[i][j] * kg[j];
             }
             gkv += gtd[i] * diffusion;
             grh -= gtd[i];
+#pragma unroll
+            for (int j = i; j < 4; ++j) {
+                H[i][j] = kg[i] * Tn[j] + kg[j] * Tn[i];
+                H[j][i] = H[i][j];
+            }
         }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                double acc = 0;
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) acc += H[m][kk] * sh[c][kk];
+                gsh[c][m] += acc;
+            }
         a.g[(size_t)DES_EF_THERM_COND * ne + e] += gkv * vol;
         gvol += gkv * k + grh * hrcp;
     }
