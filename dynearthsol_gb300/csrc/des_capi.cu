@@ -668,13 +668,20 @@ constexpr int MAX_STATE_FIELDS = 22;
 
 // download of every non-NULL field; with `early`, the fields the step's tail
 // does not write are copied once the step records ev_mid (the step must have
-// been launched from step_exec_mid), while the tail kernels still run
-int download_state(des_ctx *c, des_host_state *st, bool early)
+// been launched from step_exec_mid), while the tail kernels still run.  With
+// `after_step`, coord0 and (outside plane strain) stressyy are skipped: no
+// step writes them, so the host arrays they were uploaded from hold them.
+int download_state(des_ctx *c, des_host_state *st, bool early, bool after_step = false)
 {
     int rc;
     if ((rc = ensure_xfer(c))) return rc;
+    des_host_state out = *st;
+    if (after_step) {
+        out.coord0 = nullptr;
+        if (!c->kp.mat.is_plane_strain) out.stressyy = nullptr;
+    }
     StateField f[MAX_STATE_FIELDS];
-    const int nf = state_fields(c, st, f);
+    const int nf = state_fields(c, &out, f);
     Pipe pp{c, false};
     if (early) {
         if ((rc = pp.begin(c->ev_mid))) return rc;
@@ -1094,16 +1101,25 @@ int des_step(des_ctx *c, int nsteps)
 int des_step_host(des_ctx *c, des_host_state *st, int nsteps)
 {
     if (!c || !st || nsteps < 0) return DES_EINPUT;
-    int rc = des_upload_state(c, st);
-    if (rc) return rc;
-    if (nsteps == 0) return download_state(c, st, false);
+    int rc;
+    if (nsteps == 0) {
+        if ((rc = des_upload_state(c, st))) return rc;
+        return download_state(c, st, false);
+    }
+    // The first step writes strain_rate, force, dpressure, edvoldt and ntmp
+    // before it reads them (element pass, force, stress, stress, node pass),
+    // so their host values cannot change the result: they are not uploaded,
+    // and the download brings back their new values.
+    des_host_state in = *st;
+    in.strain_rate = in.force = in.dpressure = in.edvoldt = in.ntmp = nullptr;
+    if ((rc = des_upload_state(c, &in))) return rc;
     // the last step comes from the graph that records ev_mid, so that the
     // fields it no longer writes go back to the host while its tail runs
     if ((rc = des_step(c, nsteps - 1))) return rc;
     if (!c->step_exec_mid && (rc = build_step_graph(c, c->ev_mid))) return rc;
     CK(cudaGraphLaunch(c->step_exec_mid, c->stream));
     c->launches += c->step_kernels;
-    return download_state(c, st, true);
+    return download_state(c, st, true, true);
 }
 
 int des_synchronize(des_ctx *c)
