@@ -132,11 +132,12 @@ __device__ __forceinline__ double trace_(const double *s)
 // of x / 3.  The exact quotient of a 53-bit significand by 3 has a
 // fractional part, in units of the quotient's last place, of 0, 1/3 or 2/3,
 // so it lies at least 1/6 ulp from every rounding midpoint, and the fma
-// rounds to the IEEE quotient: the result is bit-identical to x / 3.  Below
-// |x| = 2^-900, where x * YL could lose bits to underflow, it divides.  The
-// test |x| < 2^-900 reads the exponent field (biased exponent < 123) with
-// integer instructions, which keeps it off the FP64 pipe; it is true for the
-// same x, NaN included, as fabs(x) < 0x1p-900.
+// rounds to the IEEE quotient: the result is bit-identical to x / 3.  For a
+// nonzero |x| below 2^-900, where x * YL could lose bits to underflow, it
+// divides; +-0 takes the fma path, which returns it unchanged, as 0 / 3 does
+// (the step divides exact zeros often: a pressure correction that vanishes).
+// The tests read the exponent and mantissa bits with integer instructions,
+// off the FP64 pipe.
 __device__ __forceinline__ unsigned biased_exponent(double x)
 {
     return ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
@@ -146,7 +147,8 @@ __device__ __forceinline__ double div3(double x)
 {
     constexpr double YH = 0x1.5555555555555p-2;    // RN(1/3)
     constexpr double YL = 0x1.5555555555555p-56;   // RN(1/3 - YH)
-    if (biased_exponent(x) < 123u) return x / 3;
+    const unsigned mag_hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
+    if (mag_hi < (123u << 20) && (mag_hi | (unsigned)__double2loint(x)) != 0) return x / 3;
     return fma(x, YH, x * YL);
 }
 

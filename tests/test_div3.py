@@ -1,5 +1,6 @@
 """div3 (csrc/des_common.cuh): x / 3 as fma(x, YH, x * YL) is bit-identical
-to the IEEE quotient for |x| >= 2^-900 (the kernels divide below that).
+to the IEEE quotient for |x| >= 2^-900 and for +-0 (the kernels divide the
+nonzero values below 2^-900).
 
 The argument is in the kernel's comment; here the same two operations run
 through the C library's fma, which is correctly rounded like the device's
@@ -27,7 +28,7 @@ def _bits(x):
 
 
 def _div3(x):
-    if abs(x) < 2.0 ** -900:
+    if abs(x) < 2.0 ** -900 and x != 0:   # +-0 takes the fma path
         return x / 3
     return _libm.fma(x, YH, x * YL)
 
