@@ -370,9 +370,9 @@ def main():
     if args.precision == "mixed" and not args.no_compare and args.gate_steps > 0:
         gate = error_gate(wl, init, clock0, cp, stream, args.gate_steps)
 
-    # ---- dominant kernel alone, for the roofline ----
-    m.upload(init, clock0)
-    m.step(2)
+    # ---- dominant kernel alone, for the roofline: its per-function form (a
+    # kernel inside the step's graph cannot be timed with events) on the state
+    # the timed steps left, so that it sees the same mix of elements ----
     k_ms = kernel_time(m, stream, "update_stress")
     hbm_peak, peak_kind = measured_peaks()
     alg = STRESS_BYTES_PER_ELEM_FP64 * ne + 16 * nn

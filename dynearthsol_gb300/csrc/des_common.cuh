@@ -38,7 +38,7 @@ struct Clock {
     // compute_dt accumulators: min over elements as ordered bit patterns
     unsigned long long red_minh;
     unsigned long long red_maxwell;
-    unsigned long long red_diffusion;
+    unsigned long long red_diffusion;   // unused: the diffusion time comes from red_minh
     double last_dt_terms[4];   // maxwell, diffusion, advection, elastic
 };
 
@@ -510,6 +510,24 @@ __device__ __forceinline__ double tri_area(const double *a, const double *b, con
     double d1 = ab2 * ac0 - ab0 * ac2;
     double d2 = ab0 * ac1 - ab1 * ac0;
     return sqrt(d0 * d0 + d1 * d1 + d2 * d2) / 2;
+}
+
+// (2 x area of triangle abc)^2 in 3D: tri_area<3> is sqrt of this over 2
+__device__ __forceinline__ double tri_area2_3d(const double *a, const double *b, const double *c)
+{
+    double ab0 = b[0] - a[0], ab1 = b[1] - a[1], ab2 = b[2] - a[2];
+    double ac0 = c[0] - a[0], ac1 = c[1] - a[1], ac2 = c[2] - a[2];
+    double d0 = ab1 * ac2 - ab2 * ac1;
+    double d1 = ab2 * ac0 - ab0 * ac2;
+    double d2 = ab0 * ac1 - ab1 * ac0;
+    return d0 * d0 + d1 * d1 + d2 * d2;
+}
+
+// the Maxwell time 0.5 visc_min / shearm is the same for every element: one
+// material without markers or a per-element shear modulus
+__device__ __forceinline__ bool uniform_maxwell_time(const KP &p)
+{
+    return p.mat.nmat == 1 && !p.emark && !p.ef[DES_EF_SHEAR_MODULUS];
 }
 
 template <int ND>

@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
     bool do_dt = (flags & GEO_DT) != 0;
     if (flags & GEO_DT_IF_STEP) do_dt = do_dt && (p.clk->steps % 10 == 0);
     do_dt = do_dt && p.prm.fixed_dt == 0;
-    unsigned long long b_minh = ~0ull, b_maxwell = ~0ull, b_diff = ~0ull;
+    unsigned long long b_minh = ~0ull, b_maxwell = ~0ull;
     if (in) {
         double c[NPE][ND];
         int nodes[NPE];
@@ -776,9 +776,13 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
             // compute_dt element terms (geometry.cxx:254-292)
             double minh;
             if (ND == 3) {
-                double maxa = dmax_(dmax_(tri_area<3>(c[0], c[1], c[2]), tri_area<3>(c[0], c[1], c[NPE - 1])),
-                                    dmax_(tri_area<3>(c[2], c[NPE - 1], c[0]),
-                                          tri_area<3>(c[2], c[NPE - 1], c[1])));
+                // the largest face area: sqrt is correctly rounded and
+                // monotonic and /2 exact, so max_i sqrt(s_i) / 2 equals
+                // sqrt(max_i s_i) / 2 -- one square root instead of four
+                const double s2 = dmax_(dmax_(tri_area2_3d(c[0], c[1], c[2]), tri_area2_3d(c[0], c[1], c[NPE - 1])),
+                                        dmax_(tri_area2_3d(c[2], c[NPE - 1], c[0]),
+                                              tri_area2_3d(c[2], c[NPE - 1], c[1])));
+                double maxa = sqrt(s2) / 2;
                 minh = 3 * vol / maxa;
             } else {
                 double d01 = 0, d12 = 0, d02 = 0;
@@ -792,16 +796,16 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
                 double maxl = sqrt(dmax_(dmax_(d01, d12), d02));
                 minh = 2 * vol / maxl;
             }
-            double tmax = 0.5 * p.mat.visc_min / (1e-40 + m_shearm(p, e));
             b_minh = dbits(minh);
-            b_maxwell = dbits(tmax);
-            if (p.prm.has_thermal_diffusion) b_diff = dbits(0.5 * minh * minh / p.mat.therm_diff_max);
+            // uniform, the Maxwell time is formed once by k_dt_finalize
+            if (!uniform_maxwell_time(p)) b_maxwell = dbits(0.5 * p.mat.visc_min / (1e-40 + m_shearm(p, e)));
+            // the diffusion time 0.5 minh^2 / kappa is non-decreasing in minh,
+            // so its minimum over the elements is k_dt_finalize's 0.5 min(minh)^2 / kappa
         }
     }
     if (do_dt) {   // uniform across the grid: every thread reaches the shuffles
         warp_block_min<ND>(b_minh, &p.clk->red_minh);
-        warp_block_min<ND>(b_maxwell, &p.clk->red_maxwell);
-        warp_block_min<ND>(b_diff, &p.clk->red_diffusion);
+        if (!uniform_maxwell_time(p)) warp_block_min<ND>(b_maxwell, &p.clk->red_maxwell);
     }
 }
 
@@ -816,9 +820,12 @@ __global__ void k_dt_finalize(KP p, int only_on_step)
         dt = p.prm.fixed_dt;
     } else {
         double minl = bitsd(ck->red_minh);
-        double dt_maxwell = ck->red_maxwell == ~0ull ? DBL_MAX : bitsd(ck->red_maxwell);
-        double dt_diffusion = ck->red_diffusion == ~0ull ? DBL_MAX : bitsd(ck->red_diffusion);
-        if (ck->red_minh == ~0ull) minl = DBL_MAX;
+        const bool any = ck->red_minh != ~0ull;
+        if (!any) minl = DBL_MAX;
+        double dt_maxwell;
+        if (uniform_maxwell_time(p)) dt_maxwell = any ? 0.5 * p.mat.visc_min / (1e-40 + m_shearm(p, 0)) : DBL_MAX;
+        else dt_maxwell = ck->red_maxwell == ~0ull ? DBL_MAX : bitsd(ck->red_maxwell);
+        double dt_diffusion = (any && p.prm.has_thermal_diffusion) ? 0.5 * minl * minl / p.mat.therm_diff_max : DBL_MAX;
         double dt_advection = 0.5 * minl / p.prm.max_vbc_val;
         double dt_elastic = p.prm.is_quasi_static
             ? 0.5 * minl / (p.prm.max_vbc_val * p.prm.inertial_scaling)
