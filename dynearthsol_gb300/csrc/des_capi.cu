@@ -76,6 +76,11 @@ void invalidate_graph(des_ctx *c)
         cudaGraphExecDestroy(c->step_exec_mid);
         c->step_exec_mid = nullptr;
     }
+    if (c->pipe_exec) {
+        cudaGraphExecDestroy(c->pipe_exec);
+        c->pipe_exec = nullptr;
+    }
+    c->pipe_key.clear();
 }
 
 void set_rho_pseudo(des_ctx *c);
@@ -146,6 +151,47 @@ void set_rho_pseudo(des_ctx *c)
 }
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Slabs of the pipelined host step: B element blocks of equal index ranges,
+// node block b starting at the smallest node of element block b.  Usable
+// when every element's nodes lie in its node block or the next, and every
+// node's support elements in its element block or the previous one: then a
+// node pass on block b reads element blocks b-1 and b, and an element pass
+// on block b reads node blocks b and b+1.  Meshes numbered slab by slab (the
+// structured box meshes: x is the slowest index of both numberings) qualify.
+bool slab_partition(int B, const int *cn, int ne, int npe, int nn, const std::vector<int> &sup_off,
+                    const std::vector<int> &sup_ent, std::vector<int> &eb, std::vector<int> &nb)
+{
+    if (B < 2 || ne < B) return false;
+    eb.assign(B + 1, 0);
+    nb.assign(B + 1, 0);
+    for (int b = 0; b <= B; ++b) eb[b] = (int)((long long)ne * b / B);
+    for (int b = 1; b < B; ++b) {
+        int m = nn;
+        for (int e = eb[b]; e < eb[b + 1]; ++e)
+            for (int i = 0; i < npe; ++i) m = std::min(m, cn[(size_t)e * npe + i]);
+        nb[b] = m;
+    }
+    nb[0] = 0;
+    nb[B] = nn;
+    for (int b = 0; b < B; ++b)
+        if (nb[b + 1] <= nb[b]) return false;
+    for (int b = 0; b < B; ++b) {
+        const int hi = nb[std::min(b + 2, B)];
+        for (int e = eb[b]; e < eb[b + 1]; ++e)
+            for (int i = 0; i < npe; ++i) {
+                const int n = cn[(size_t)e * npe + i];
+                if (n < nb[b] || n >= hi) return false;
+            }
+        const int elo = eb[std::max(b - 1, 0)], ehi = eb[b + 1];
+        for (int n = nb[b]; n < nb[b + 1]; ++n)
+            for (int q = sup_off[n]; q < sup_off[n + 1]; ++q) {
+                const int e = sup_ent[q] >> 2;
+                if (e < elo || e >= ehi) return false;
+            }
+    }
+    return true;
+}
 
 }  // namespace
 
@@ -247,6 +293,32 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
         }
     }
 
+    // fine slabs of the pipelined host step (the largest valid count) and the
+    // boundary facets grouped by the fine slab of their element; coarse slabs
+    // (8, else 4) of at least 4 fine slabs each
+    std::vector<int> fac_order;
+    for (int F : {256, 192, 160, 128, 96, 80, 64, 48, 40, 32, 24, 20, 16}) {
+        if (F * 4 > ne) continue;
+        if (slab_partition(F, cn, ne, npe, nn, sup_off, sup_ent, c->slab_e, c->slab_n)) {
+            c->nfine = F;
+            break;
+        }
+    }
+    if (c->nfine >= 32) c->nslab = 8;
+    else if (c->nfine >= 16) c->nslab = 4;
+    if (c->nslab > 1) {
+        const int F = c->nfine;
+        std::vector<int> blk(std::max(nbf, 1), 0);
+        for (int q = 0; q < nbf; ++q)
+            blk[q] = (int)(std::upper_bound(c->slab_e.begin(), c->slab_e.end(), fac_elem[q]) - c->slab_e.begin()) - 1;
+        fac_order.resize(nbf);
+        for (int q = 0; q < nbf; ++q) fac_order[q] = q;
+        std::stable_sort(fac_order.begin(), fac_order.end(), [&](int a, int b) { return blk[a] < blk[b]; });
+        c->slab_f.assign(F + 1, 0);
+        for (int q = 0; q < nbf; ++q) c->slab_f[blk[q] + 1]++;
+        for (int b = 0; b < F; ++b) c->slab_f[b + 1] += c->slab_f[b];
+    }
+
     // ---- device ----
     if (cudaGetDevice(&c->device) != cudaSuccess) {
         int code = fail_msg(g_create_error, DES_ECUDA, "no CUDA device");
@@ -281,6 +353,7 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     add((void **)&d_fe, fac_elem.size() * I);
     add((void **)&d_ff, fac_f.size() * I);
     add((void **)&d_fb, fac_bdry.size() * I);
+    if (c->nslab > 1) add((void **)&c->d_fac_order, std::max<size_t>(fac_order.size(), 1) * I);
     if (mat->elemmarkers && mat->nmat > 1) add((void **)&d_emark, (size_t)ne * mat->nmat * I);
     add((void **)&p.x, (size_t)nn * nd * D);
     add((void **)&p.x0, (size_t)nn * nd * D);
@@ -371,6 +444,8 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     p.hc = d_hc;
     p.qv = d_qv;
     p.hc64 = d_hc64;
+    p.e_lo = 0, p.e_hi = ne, p.n_lo = 0, p.n_hi = nn, p.f_lo = 0, p.f_hi = nbf;
+    p.fac_order = nullptr;
     p.tape_visc = nullptr;
     p.tape_evp = nullptr;
     for (int i = 0; i < DES_NBDRYTYPES; ++i)
@@ -396,6 +471,7 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     up(d_fe, fac_elem.data(), fac_elem.size() * I);
     up(d_ff, fac_f.data(), fac_f.size() * I);
     up(d_fb, fac_bdry.data(), fac_bdry.size() * I);
+    if (c->d_fac_order && !fac_order.empty()) up(c->d_fac_order, fac_order.data(), fac_order.size() * I);
     if (d_emark) {
         std::vector<int> em((size_t)ne * mat->nmat);
         for (int e = 0; e < ne; ++e)
@@ -454,6 +530,11 @@ int des_destroy(des_ctx *c)
     cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
     adj_free(c);
+    if (c->ystream) {
+        cudaStreamSynchronize(c->ystream);
+        cudaStreamDestroy(c->ystream);
+        for (cudaEvent_t e : c->pipe_ev) cudaEventDestroy(e);
+    }
     if (c->xstream) {
         cudaStreamSynchronize(c->xstream);
         cudaStreamDestroy(c->xstream);
@@ -1085,6 +1166,272 @@ int build_step_graph(des_ctx *c, cudaEvent_t mid = nullptr)
 
 }  // namespace
 
+// ---- the slab-pipelined host step ----
+namespace {
+
+// A field of the pipelined host step: host rows, device SoA array (and its
+// FP32 copy for the mixed shape functions), values per row, node or element
+// rows, whether it is uploaded / downloaded, and its staging region.
+struct SlabField {
+    double *host;
+    double *dev;
+    float *dev32;
+    int ncomp;
+    bool node, up, down;
+    double *stage;
+};
+
+// The fields of one call, or false when the call does not qualify: the
+// state must be complete (the derived fields and coord0 given, as the
+// reference's Variables hold them) and page-locked (graph copy nodes).
+bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &out)
+{
+    KP &p = c->kp;
+    const int nd = c->nd, npe = c->npe, nstr = c->nstr, ne = c->ne;
+    const size_t shp1 = (size_t)ne * npe;
+    float *s32 = use_mixed(c) ? p.shp32 : nullptr;
+    const bool ps = p.mat.is_plane_strain != 0;
+    // up: needed by the step; down: written by it (strain_rate, force,
+    // dpressure, edvoldt and ntmp are written before they are read; coord0
+    // and, outside plane strain, stressyy are never written)
+    const SlabField all[] = {
+        {st->coord, p.x, nullptr, nd, true, true, true, nullptr},
+        {st->coord0, p.x0, nullptr, nd, true, true, false, nullptr},
+        {st->vel, p.v, nullptr, nd, true, true, true, nullptr},
+        {st->force, p.f, nullptr, nd, true, false, true, nullptr},
+        {st->temperature, p.T, nullptr, 1, true, true, true, nullptr},
+        {st->mass, p.mass, nullptr, 1, true, true, true, nullptr},
+        {st->tmass, p.tmass, nullptr, 1, true, true, true, nullptr},
+        {st->volume_n, p.vol_n, nullptr, 1, true, true, true, nullptr},
+        {st->ntmp, p.ntmp, nullptr, 1, true, false, true, nullptr},
+        {st->volume, p.vol, nullptr, 1, false, true, true, nullptr},
+        {st->volume_old, p.vol_old, nullptr, 1, false, true, true, nullptr},
+        {st->stress, p.stress, nullptr, nstr, false, true, true, nullptr},
+        {st->strain, p.strain, nullptr, nstr, false, true, true, nullptr},
+        {st->strain_rate, p.srate, nullptr, nstr, false, false, true, nullptr},
+        {st->plstrain, p.pls, nullptr, 1, false, true, true, nullptr},
+        {st->delta_plstrain, p.dpls, nullptr, 1, false, true, true, nullptr},
+        {st->stressyy, p.syy, nullptr, 1, false, true, ps, nullptr},
+        {st->dpressure, p.dp, nullptr, 1, false, false, true, nullptr},
+        {st->edvoldt, p.edvoldt, nullptr, 1, false, false, true, nullptr},
+        {st->shpdx, p.shp, s32, npe, false, true, true, nullptr},
+        {nd == 3 ? st->shpdy : nullptr, p.shp + shp1, s32 ? s32 + shp1 : nullptr, npe, false, nd == 3, nd == 3, nullptr},
+        {st->shpdz, p.shp + (size_t)(nd - 1) * shp1, s32 ? s32 + (size_t)(nd - 1) * shp1 : nullptr, npe, false, true, true,
+         nullptr},
+    };
+    out.clear();
+    size_t off = 0;
+    for (SlabField f : all) {
+        if (!f.up && !f.down) continue;
+        if (!f.host) {
+            if (f.up) return false;   // an input is missing: the general path
+            continue;
+        }
+        const size_t cnt = (size_t)(f.node ? c->nn : c->ne) * f.ncomp;
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, f.host) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+            cudaGetLastError();
+            return false;
+        }
+        if (f.ncomp > 1) {
+            if (off + cnt > c->xstage_doubles) return false;
+            f.stage = c->d_xstage + off;
+            off += cnt;
+        }
+        out.push_back(f);
+    }
+    return true;
+}
+
+// One step with the host transfers pipelined over the slabs (captured into
+// c->pipe_exec).  The mesh is cut into F fine slabs (element and node index
+// ranges such that an element's nodes lie in its fine slab or the next and a
+// node's support elements in its fine slab or the previous one) and B coarse
+// slabs of fine slabs [C_b, C_b+1).  The step's eight stages alternate
+// between element passes (reading the node slabs j, j+1 for element slab j)
+// and node passes (reading the element slabs j-1, j for node slab j).  Stage
+// s of coarse slab b covers the fine slabs [C_b - g_s, C_b+1 - g_s), with the
+// skew g = 0,0,1,1,2,2,3,3: every stage then reads only what the stages of
+// coarse slabs <= b have written, and writes nothing that a stage of a later
+// slab, run afterwards, still has to read in its old state (each element pass
+// lies one fine slab behind the node pass before it).  So the slabs run one
+// after the other on the compute stream, while three streams overlap:
+// uploads (xstream), coarse slab b uploads the element fine slabs [C_b,
+// C_b+1) and the node fine slabs [C_b + 1, C_b+1 + 1), all that slab b's first
+// stage reads; downloads (ystream), once slab b has run, the fine slabs
+// [C_b - 3, C_b+1 - 3), which no later stage writes.
+int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec_t *exec, int *nkern)
+{
+    const int B = c->nslab, NF = c->nfine;
+    const bool mixed = use_mixed(c);
+    const KP p0 = step_kp(c);
+    const bool thermal = p0.prm.has_thermal_diffusion != 0;
+    cudaStream_t cs = c->stream, xs = c->xstream, ys = c->ystream;
+    std::vector<cudaEvent_t> &ev = c->pipe_ev;   // [0,B) uploaded, [B,2B) slab done, 2B fork, 2B+1/2 joins
+    static const int SKEW[8] = {0, 0, 1, 1, 2, 2, 3, 3};
+    auto cb = [&](int b) { return (int)((long long)NF * b / B); };   // C_b
+    // a fine-slab range, clipped to [0, NF); the last coarse slab runs to NF
+    auto fine = [&](int b, int shift, int &lo, int &hi) {
+        lo = b == 0 ? 0 : std::max(0, cb(b) - shift);
+        hi = b == B - 1 ? NF : std::min(NF, cb(b + 1) - shift);
+    };
+    int n = 0;
+    CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+#define CKC(call)                                \
+    do {                                         \
+        if ((e = (call)) != cudaSuccess) goto end; \
+    } while (0)
+    CKC(cudaEventRecord(ev[2 * B], cs));
+    CKC(cudaStreamWaitEvent(xs, ev[2 * B], 0));
+    CKC(cudaStreamWaitEvent(ys, ev[2 * B], 0));
+    // uploads
+    for (int b = 0; b < B; ++b) {
+        int elo, ehi, nlo, nhi;
+        fine(b, 0, elo, ehi);
+        fine(b, -1, nlo, nhi);
+        RowTable t{};
+        for (const SlabField &f : F) {
+            if (!f.up) continue;
+            const int lo = f.node ? c->slab_n[nlo] : c->slab_e[elo], hi = f.node ? c->slab_n[nhi] : c->slab_e[ehi];
+            if (hi <= lo) continue;
+            const size_t o = (size_t)lo * f.ncomp, bytes = (size_t)(hi - lo) * f.ncomp * sizeof(double);
+            CKC(cudaMemcpyAsync((f.ncomp == 1 ? f.dev : f.stage) + o, f.host + o, bytes, cudaMemcpyHostToDevice, xs));
+            if (f.ncomp > 1) {
+                RowField &r = t.f[t.count++];
+                r = {f.stage, f.dev, f.dev32, t.total, f.node ? c->nn : c->ne, f.ncomp, lo, hi};
+                t.total += (long long)(hi - lo) * f.ncomp;
+            }
+        }
+        n += launch_rows(t, true, xs);
+        CKC(cudaGetLastError());
+        CKC(cudaEventRecord(ev[b], xs));
+    }
+    // the step, coarse slab by coarse slab
+    for (int b = 0; b < B; ++b) {
+        CKC(cudaStreamWaitEvent(cs, ev[b], 0));
+        for (int st = 0; st < 8; ++st) {
+            int lo, hi;
+            fine(b, SKEW[st], lo, hi);
+            if (hi <= lo) continue;
+            KP q = p0;
+            q.e_lo = c->slab_e[lo], q.e_hi = c->slab_e[hi];
+            q.n_lo = c->slab_n[lo], q.n_hi = c->slab_n[hi];
+            q.f_lo = c->slab_f[lo], q.f_hi = c->slab_f[hi];
+            q.fac_order = c->d_fac_order;
+            switch (st) {
+            case 0: n += mixed ? launch_elem_pass_mixed(q, cs, thermal) : launch_elem_pass(q, cs, thermal); break;
+            case 1: n += mixed ? launch_node_pass_mixed(q, cs, thermal) : launch_node_pass(q, cs, thermal); break;
+            case 2: n += mixed ? launch_update_stress_mixed(q, cs, true) : launch_update_stress(q, cs, true); break;
+            case 3: n += launch_nmd_gather(q, cs); break;
+            case 4: n += launch_nmd_correct(q, cs, true); break;
+            case 5: n += launch_force(q, cs, true, mixed); break;
+            case 6: {
+                int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP | GEO_MASS_TERMS;
+                if (q.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;
+                n += launch_geometry(q, cs, geo);
+                break;
+            }
+            case 7: n += launch_mass_sum(q, cs); break;
+            }
+            CKC(cudaGetLastError());
+        }
+        CKC(cudaEventRecord(ev[B + b], cs));
+    }
+    n += launch_dt_finalize(p0, cs, true);
+    CKC(cudaGetLastError());
+    // downloads
+    for (int b = 0; b < B; ++b) {
+        CKC(cudaStreamWaitEvent(ys, ev[B + b], 0));
+        int flo, fhi;
+        fine(b, 3, flo, fhi);
+        RowTable t{};
+        for (const SlabField &f : F) {
+            if (!f.down || f.ncomp == 1) continue;
+            const int lo = f.node ? c->slab_n[flo] : c->slab_e[flo], hi = f.node ? c->slab_n[fhi] : c->slab_e[fhi];
+            if (hi <= lo) continue;
+            RowField &r = t.f[t.count++];
+            r = {f.stage, f.dev, nullptr, t.total, f.node ? c->nn : c->ne, f.ncomp, lo, hi};
+            t.total += (long long)(hi - lo) * f.ncomp;
+        }
+        n += launch_rows(t, false, ys);
+        CKC(cudaGetLastError());
+        for (const SlabField &f : F) {
+            if (!f.down) continue;
+            const int lo = f.node ? c->slab_n[flo] : c->slab_e[flo], hi = f.node ? c->slab_n[fhi] : c->slab_e[fhi];
+            if (hi <= lo) continue;
+            const size_t o = (size_t)lo * f.ncomp, bytes = (size_t)(hi - lo) * f.ncomp * sizeof(double);
+            CKC(cudaMemcpyAsync(f.host + o, (f.ncomp == 1 ? f.dev : f.stage) + o, bytes, cudaMemcpyDeviceToHost, ys));
+        }
+    }
+    CKC(cudaEventRecord(ev[2 * B + 1], xs));
+    CKC(cudaEventRecord(ev[2 * B + 2], ys));
+    CKC(cudaStreamWaitEvent(cs, ev[2 * B + 1], 0));
+    CKC(cudaStreamWaitEvent(cs, ev[2 * B + 2], 0));
+end:
+#undef CKC
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        *exec = nullptr;
+        return cuda_fail(c, e, "pipelined host step capture");
+    }
+    *nkern = n;
+    return DES_OK;
+}
+
+int ensure_pipe(des_ctx *c)
+{
+    if (c->ystream) return DES_OK;
+    c->pipe_ev.assign(2 * c->nslab + 3, nullptr);
+    for (cudaEvent_t &e : c->pipe_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&c->ystream, cudaStreamNonBlocking));
+    return DES_OK;
+}
+
+// des_step_host for one step over the slabs; *done false: not applicable
+int step_host_pipelined(des_ctx *c, des_host_state *st, bool *done)
+{
+    *done = false;
+    if (c->nslab < 2) return DES_OK;
+    int rc;
+    if ((rc = ensure_xfer(c)) || (rc = ensure_pipe(c))) return rc;
+    std::vector<SlabField> F;
+    if (!slab_fields(c, st, F)) return DES_OK;
+    std::vector<const void *> key;
+    for (const SlabField &f : F) key.push_back(f.host);
+    if (!c->pipe_exec || key != c->pipe_key) {
+        if (c->pipe_exec) {
+            cudaGraphExecDestroy(c->pipe_exec);
+            c->pipe_exec = nullptr;
+        }
+        if ((rc = capture_pipelined(c, F, &c->pipe_exec, &c->pipe_kernels))) return rc;
+        c->pipe_key = key;
+    }
+    // the clock, as des_upload_state sets it
+    Clock ck{};
+    ck.time = st->time;
+    ck.dt = st->dt;
+    ck.steps = st->steps;
+    ck.red_minh = ck.red_maxwell = ck.red_diffusion = ~0ull;
+    CK(cudaMemcpyAsync(c->kp.clk, &ck, sizeof ck, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaGraphLaunch(c->pipe_exec, c->stream));
+    c->launches += c->pipe_kernels;
+    CK(cudaMemcpyAsync(&ck, c->kp.clk, sizeof ck, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    st->time = ck.time;
+    st->dt = ck.dt;
+    st->steps = ck.steps;
+    c->has_state = true;
+    *done = true;
+    return DES_OK;
+}
+
+}  // namespace
+
 int des_step(des_ctx *c, int nsteps)
 {
     if (!c || nsteps < 0) return DES_EINPUT;
@@ -1102,6 +1449,11 @@ int des_step_host(des_ctx *c, des_host_state *st, int nsteps)
 {
     if (!c || !st || nsteps < 0) return DES_EINPUT;
     int rc;
+    if (nsteps == 1) {   // transfers overlapped with the step, slab by slab
+        bool done = false;
+        if ((rc = step_host_pipelined(c, st, &done))) return rc;
+        if (done) return DES_OK;
+    }
     if (nsteps == 0) {
         if ((rc = des_upload_state(c, st))) return rc;
         return download_state(c, st, false);

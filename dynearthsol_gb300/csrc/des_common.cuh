@@ -80,6 +80,12 @@ struct MatC {
 // Everything a kernel needs, passed by value.
 struct KP {
     int nd, npe, nstr, nn, ne, nbf;
+    // index ranges of one launch of the fused step's kernels: elements
+    // [e_lo, e_hi), nodes [n_lo, n_hi), boundary facets fac_order[f_lo, f_hi)
+    // (fac_order null: the facet itself); the whole mesh outside the
+    // slab-pipelined host step
+    int e_lo, e_hi, n_lo, n_hi, f_lo, f_hi;
+    const int *fac_order;
     // mesh
     const int *conn;
     const unsigned *bcflag;

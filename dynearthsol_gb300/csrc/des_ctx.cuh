@@ -2,6 +2,7 @@
 // library: des_capi.cu and the adjoint's host side share it).
 #pragma once
 #include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -39,6 +40,18 @@ struct des_ctx {
     size_t xstage_doubles = 0;
     cudaEvent_t ev_mid = nullptr;     // recorded by step_exec_mid once nmd_correct is done
     cudaGraphExec_t step_exec_mid = nullptr;
+    // slabs of the pipelined host step (des_step_host): nfine fine slabs of
+    // element rows [slab_e[j], slab_e[j+1]), node rows [slab_n[j],
+    // slab_n[j+1]) and boundary facets d_fac_order[slab_f[j] .. slab_f[j+1]);
+    // nslab coarse slabs of whole fine slabs; nslab 1: not pipelined
+    int nfine = 0, nslab = 1;
+    std::vector<int> slab_e, slab_n, slab_f;
+    int *d_fac_order = nullptr;
+    cudaStream_t ystream = nullptr;        // device -> host copies of the pipelined step
+    cudaGraphExec_t pipe_exec = nullptr;   // the pipelined host step, for the host arrays below
+    std::vector<const void *> pipe_key;
+    std::vector<cudaEvent_t> pipe_ev;
+    int pipe_kernels = 0;
     int step_kernels = 0;
     long long launches = 0;
     std::string err;

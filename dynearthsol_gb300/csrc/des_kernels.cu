@@ -156,12 +156,12 @@ template <int ND>
 __global__ void __launch_bounds__(TPB) k_elem_pass(KP p, int heat)
 {
     constexpr int NPE = ND + 1, NSTR = ND * (ND + 1) / 2;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int e = p.e_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (e == 0) {   // var.steps++; var.time += var.dt (dynearthsol.cxx:325-326)
         p.clk->steps += 1;
         p.clk->time += p.clk->dt;
     }
-    if (e >= p.ne) return;
+    if (e >= p.e_hi) return;
     const size_t ne = p.ne;
     double sr[NSTR];
     strain_rate_elem<ND>(p, e, sr);
@@ -203,8 +203,8 @@ __global__ void __launch_bounds__(TPB) k_elem_pass(KP p, int heat)
 template <int ND>
 __global__ void __launch_bounds__(TPB) k_node_pass(KP p, int heat)
 {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= p.nn) return;
+    const int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.n_hi) return;
     const size_t ne = p.ne;
     double tdot = 0, dvoldt = 0;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
@@ -253,8 +253,8 @@ template <int ND>
 __global__ void __launch_bounds__(TPB) k_update_stress(KP p, int fused)
 {
     constexpr int NSTR = ND * (ND + 1) / 2;
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= p.ne) return;
+    int e = p.e_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.e_hi) return;
     const size_t ne = p.ne;
     double edv;
     if (fused) {
@@ -302,8 +302,8 @@ __global__ void __launch_bounds__(TPB) k_update_stress(KP p, int fused)
 template <int ND>
 __global__ void __launch_bounds__(TPB) k_nmd_gather(KP p)
 {
-    int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= p.nn) return;
+    int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.n_hi) return;
     double acc = 0;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
         int e = p.sup_ent[q] >> 2;
@@ -378,9 +378,9 @@ __device__ void facet_force(const KP &p, int q)
 template <int ND>
 __global__ void __launch_bounds__(TPB) k_nmd_correct(KP p, int with_facets)
 {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < p.ne) {
-        const int e = t;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, nel = p.e_hi - p.e_lo;
+    if (t < nel) {
+        const int e = p.e_lo + t;
         double dpn = 0;
 #pragma unroll
         for (int i = 0; i < ND + 1; ++i) dpn += p.ntmp[conn_at(p, i, e)];
@@ -388,8 +388,9 @@ __global__ void __launch_bounds__(TPB) k_nmd_correct(KP p, int with_facets)
         double dp_orig = p.dp[e];
 #pragma unroll
         for (int i = 0; i < ND; ++i) p.stress[(size_t)i * p.ne + e] += divnd<ND>(-dp_orig + dp_el);
-    } else if (with_facets && t < p.ne + p.nbf) {
-        facet_force<ND>(p, t - p.ne);
+    } else if (with_facets && t < nel + (p.f_hi - p.f_lo)) {
+        const int i = p.f_lo + (t - nel);
+        facet_force<ND>(p, p.fac_order ? p.fac_order[i] : i);
     }
 }
 
@@ -443,8 +444,8 @@ __global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
 {
     constexpr int NSTR = ND * (ND + 1) / 2;
     constexpr int NPE = ND + 1;
-    int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= p.nn) return;
+    int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.n_hi) return;
     const size_t ne = p.ne;
     const double gravity = p.prm.gravity;
     double f[ND];
@@ -643,8 +644,8 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
 {
     constexpr int NSTR = ND * (ND + 1) / 2;
     constexpr int NPE = ND + 1;
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = e < p.ne;
+    int e = p.e_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = e < p.e_hi;
     const size_t ne = p.ne;
     bool do_dt = (flags & GEO_DT) != 0;
     if (flags & GEO_DT_IF_STEP) do_dt = do_dt && (p.clk->steps % 10 == 0);
@@ -879,8 +880,8 @@ __global__ void __launch_bounds__(TPB) k_mass(KP p)
 template <int ND>
 __global__ void __launch_bounds__(TPB) k_mass_sum(KP p)
 {
-    int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= p.nn) return;
+    int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.n_hi) return;
     const bool thermal = p.prm.has_thermal_diffusion;
     double vn = 0, ms = 0, tm = 0;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
@@ -1019,6 +1020,29 @@ __global__ void k_soa_to_aos(const double *__restrict__ soa, double *__restrict_
     aos[i] = soa[c * n + r];
 }
 
+// rows [lo, hi) of several fields between AoS staging and SoA arrays; a
+// thread's flat index only grows, so its field index only grows
+template <bool UP>
+__global__ void __launch_bounds__(TPB) k_rows(const __grid_constant__ RowTable t)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    int k = 0;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < t.total; g += stride) {
+        while (g >= t.f[k].first + (long long)(t.f[k].hi - t.f[k].lo) * t.f[k].nc) ++k;
+        const RowField &f = t.f[k];
+        const long long j = g - f.first;
+        const long long r = f.lo + j / f.nc, c = j % f.nc;
+        const size_t aos = (size_t)r * f.nc + c, soa = (size_t)c * f.n + r;
+        if (UP) {
+            const double v = f.stage[aos];
+            f.dev[soa] = v;
+            if (f.dev32) f.dev32[soa] = f32_of(v);
+        } else {
+            f.stage[aos] = f.dev[soa];
+        }
+    }
+}
+
 // ==================================================================
 // launchers
 // ==================================================================
@@ -1050,13 +1074,13 @@ int launch_dvoldt(const KP &p, cudaStream_t s)
 
 int launch_elem_pass(const KP &p, cudaStream_t s, bool heat)
 {
-    DISPATCH(k_elem_pass, nblocks(p.ne), p, (int)heat);
+    DISPATCH(k_elem_pass, nblocks(p.e_hi - p.e_lo), p, (int)heat);
     return 1;
 }
 
 int launch_node_pass(const KP &p, cudaStream_t s, bool heat)
 {
-    DISPATCH(k_node_pass, nblocks(p.nn), p, (int)heat);
+    DISPATCH(k_node_pass, nblocks(p.n_hi - p.n_lo), p, (int)heat);
     return 1;
 }
 
@@ -1081,19 +1105,19 @@ int launch_edvoldt(const KP &p, cudaStream_t s)
 
 int launch_update_stress(const KP &p, cudaStream_t s, bool fused)
 {
-    DISPATCH(k_update_stress, nblocks(p.ne), p, (int)fused);
+    DISPATCH(k_update_stress, nblocks(p.e_hi - p.e_lo), p, (int)fused);
     return 1;
 }
 
 int launch_nmd_gather(const KP &p, cudaStream_t s)
 {
-    DISPATCH(k_nmd_gather, nblocks(p.nn), p);
+    DISPATCH(k_nmd_gather, nblocks(p.n_hi - p.n_lo), p);
     return 1;
 }
 
 int launch_nmd_correct(const KP &p, cudaStream_t s, bool with_facets)
 {
-    long long n = p.ne + (with_facets ? p.nbf : 0);
+    long long n = (long long)(p.e_hi - p.e_lo) + (with_facets ? p.f_hi - p.f_lo : 0);
     DISPATCH(k_nmd_correct, nblocks(n), p, (int)with_facets);
     return 1;
 }
@@ -1108,11 +1132,11 @@ int launch_facet_forces(const KP &p, cudaStream_t s)
 int launch_force(const KP &p, cudaStream_t s, bool fused_motion, bool contract)
 {
     if (contract) {
-        if (p.nd == 3) k_force<3, true><<<nblocks(p.nn), TPB, 0, s>>>(p, (int)fused_motion);
-        else k_force<2, true><<<nblocks(p.nn), TPB, 0, s>>>(p, (int)fused_motion);
+        if (p.nd == 3) k_force<3, true><<<nblocks(p.n_hi - p.n_lo), TPB, 0, s>>>(p, (int)fused_motion);
+        else k_force<2, true><<<nblocks(p.n_hi - p.n_lo), TPB, 0, s>>>(p, (int)fused_motion);
         return 1;
     }
-    DISPATCH(k_force, nblocks(p.nn), p, (int)fused_motion);
+    DISPATCH(k_force, nblocks(p.n_hi - p.n_lo), p, (int)fused_motion);
     return 1;
 }
 
@@ -1148,7 +1172,7 @@ int launch_coordinate(const KP &p, cudaStream_t s, bool contract)
 
 int launch_geometry(const KP &p, cudaStream_t s, int flags)
 {
-    DISPATCH(k_geometry, nblocks(p.ne), p, flags);
+    DISPATCH(k_geometry, nblocks(p.e_hi - p.e_lo), p, flags);
     return 1;
 }
 
@@ -1160,7 +1184,7 @@ int launch_mass(const KP &p, cudaStream_t s)
 
 int launch_mass_sum(const KP &p, cudaStream_t s)
 {
-    DISPATCH(k_mass_sum, nblocks(p.nn), p);
+    DISPATCH(k_mass_sum, nblocks(p.n_hi - p.n_lo), p);
     return 1;
 }
 
@@ -1211,6 +1235,15 @@ int launch_aos_to_soa(const double *aos, double *soa, int n, int ncomp, cudaStre
 int launch_soa_to_aos(const double *soa, double *aos, int n, int ncomp, cudaStream_t s)
 {
     k_soa_to_aos<<<nblocks((long long)n * ncomp), TPB, 0, s>>>(soa, aos, n, ncomp);
+    return 1;
+}
+
+int launch_rows(const RowTable &t, bool up, cudaStream_t s)
+{
+    if (t.total <= 0) return 0;
+    const int grid = (int)(t.total < 152LL * 8 * TPB ? nblocks(t.total) : 152 * 8);
+    if (up) k_rows<true><<<grid, TPB, 0, s>>>(t);
+    else k_rows<false><<<grid, TPB, 0, s>>>(t);
     return 1;
 }
 

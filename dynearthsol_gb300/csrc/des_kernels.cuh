@@ -58,4 +58,22 @@ int launch_f64_to_f32(const double *a, float *b, long long n, cudaStream_t s);
 int launch_aos_to_soa(const double *aos, double *soa, int n, int ncomp, cudaStream_t s);
 int launch_soa_to_aos(const double *soa, double *aos, int n, int ncomp, cudaStream_t s);
 
+// The same conversion for the rows [lo, hi) of several fields in one launch
+// (one slab of the pipelined host step).  With dev32, the SoA values are also
+// written as FP32 (f32_of, as the mixed geometry pass rounds them).
+constexpr int ROWS_MAX = 12;
+struct RowField {
+    double *stage;   // AoS rows [n][nc]; rows lo..hi-1 are read (up) or written
+    double *dev;     // SoA [nc][n]
+    float *dev32;    // FP32 copy of dev, or null
+    long long first; // index of the field's first value in the launch
+    int n, nc, lo, hi;
+};
+struct RowTable {
+    RowField f[ROWS_MAX];
+    long long total;
+    int count;
+};
+int launch_rows(const RowTable &t, bool up, cudaStream_t s);
+
 }  // namespace des

@@ -129,8 +129,8 @@ __device__ __forceinline__ double dvol_mixed(const KP &p, int e)
 // update_stress (rheology.cxx:510-646), 3D, mixed precision
 __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
 {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= p.ne) return;
+    int e = p.e_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.e_hi) return;
     const size_t ne = p.ne;
     double edv;
     if (fused) {
@@ -347,12 +347,12 @@ __global__ void __launch_bounds__(TPB_M) k_heat_dvoldt_mixed3(KP p, int heat, in
 // ------------------------------------------------------------------
 __global__ void __launch_bounds__(TPB_M) k_elem_pass_mixed3(KP p, int heat)
 {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    int e = p.e_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (e == 0) {   // var.steps++; var.time += var.dt (dynearthsol.cxx:325-326)
         p.clk->steps += 1;
         p.clk->time += p.clk->dt;
     }
-    if (e >= p.ne) return;
+    if (e >= p.e_hi) return;
     const size_t ne = p.ne;
     double sr[6];
     strain_rate_mixed_elem(p, e, sr);
@@ -396,8 +396,8 @@ __global__ void __launch_bounds__(TPB_M) k_elem_pass_mixed3(KP p, int heat)
 
 __global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat)
 {
-    int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= p.nn) return;
+    int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.n_hi) return;
     const size_t ne = p.ne;
     double tdot = 0, dvoldt = 0;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat)
 
 int launch_update_stress_mixed(const KP &p, cudaStream_t s, bool fused)
 {
-    k_update_stress_mixed3<<<nblocks_m(p.ne), TPB_M, 0, s>>>(p, (int)fused);
+    k_update_stress_mixed3<<<nblocks_m(p.e_hi - p.e_lo), TPB_M, 0, s>>>(p, (int)fused);
     return 1;
 }
 
@@ -437,13 +437,13 @@ int launch_heat_and_dvoldt_mixed(const KP &p, cudaStream_t s, bool heat, bool dv
 
 int launch_elem_pass_mixed(const KP &p, cudaStream_t s, bool heat)
 {
-    k_elem_pass_mixed3<<<nblocks_m(p.ne), TPB_M, 0, s>>>(p, (int)heat);
+    k_elem_pass_mixed3<<<nblocks_m(p.e_hi - p.e_lo), TPB_M, 0, s>>>(p, (int)heat);
     return 1;
 }
 
 int launch_node_pass_mixed(const KP &p, cudaStream_t s, bool heat)
 {
-    k_node_pass_mixed3<<<nblocks_m(p.nn), TPB_M, 0, s>>>(p, (int)heat);
+    k_node_pass_mixed3<<<nblocks_m(p.n_hi - p.n_lo), TPB_M, 0, s>>>(p, (int)heat);
     return 1;
 }
 

@@ -1,0 +1,91 @@
+"""The slab-pipelined host step.
+
+With a complete, page-locked host state, des_step_host of one step overlaps
+the host transfers with the step: the mesh is cut into slabs of elements and
+nodes, slab b is uploaded while earlier slabs compute, and downloaded as soon
+as its last stage has run.  The step's stages run per slab in an order that
+respects every read and write across neighbouring slabs, so the result must
+equal upload + step + download bit for bit.  Meshes whose numbering is not
+slab by slab (permuted elements) take the general path.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    from dynearthsol_gb300 import capi
+    capi.load_library()
+
+
+def _pinned(st):
+    import torch
+    out, keep = {}, []
+    for k, v in st.items():
+        t = torch.empty(v.shape, dtype=torch.float64, pin_memory=True)
+        a = t.numpy()
+        a[...] = v
+        out[k] = a
+        keep.append(t)
+    return out, keep
+
+
+def _run(wl, precision, calls):
+    from dynearthsol_gb300.config import initial_state
+    from dynearthsol_gb300.solver import DeviceModel
+    st0, cp = initial_state(wl)
+    ref = DeviceModel(wl, comp_pressure=cp, precision=precision)
+    init = ref.init_fields(st0)
+    clk = ref.clock()
+    ref.upload({k: v.copy() for k, v in init.items()}, clk)
+    ref.step(calls)
+    want = ref.download()
+    m = DeviceModel(wl, comp_pressure=cp, precision=precision)
+    st, keep = _pinned(init)
+    c = clk
+    per_call = []
+    for _ in range(calls):
+        n0 = m.launches()
+        c = m.step_host(st, 1, c)
+        per_call.append(m.launches() - n0)
+    assert c == ref.clock()
+    for k in want:
+        np.testing.assert_array_equal(st[k], want[k], err_msg=k)
+    return per_call
+
+
+# kernel launches of one pipelined call: 8 stages per coarse slab, dt, and one
+# upload and one download conversion per coarse slab; the general path
+# launches 9 step kernels and about 20 conversions
+def _pipelined(per_call, slabs):
+    return min(per_call) >= 8 * slabs + 1 + 2 * slabs
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_pipelined_step_host_is_bit_identical(prec):
+    """16 x 6 x 4 cubes: 16 fine slabs of one x-layer, 4 coarse slabs; 12
+    calls cross the 10th step, where dt is recomputed."""
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import make_workload
+    wl = make_workload("c1_3d_evp", cells=(16, 6, 4))
+    per_call = _run(wl, capi.PREC_FP64 if prec == "fp64" else capi.PREC_MIXED, 12)
+    assert _pipelined(per_call, 4), per_call
+
+
+def test_pipelined_eight_coarse_slabs():
+    """32 x 4 x 3 cubes: 32 fine slabs, 8 coarse slabs of 4."""
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import make_workload
+    wl = make_workload("c1_3d_evp", cells=(32, 4, 3))
+    per_call = _run(wl, capi.PREC_MIXED, 12)
+    assert _pipelined(per_call, 8), per_call
+
+
+def test_permuted_mesh_takes_the_general_path():
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import make_workload
+    wl = make_workload("c4_3d_heat_jitter", cells=(16, 4, 3))
+    per_call = _run(wl, capi.PREC_MIXED, 3)
+    assert max(per_call) < 33, per_call
