@@ -74,13 +74,13 @@ def test_pipelined_step_host_is_bit_identical(prec):
     assert _pipelined(per_call, 4), per_call
 
 
-def test_pipelined_eight_coarse_slabs():
-    """32 x 4 x 3 cubes: 32 fine slabs, 8 coarse slabs of 4."""
+def test_pipelined_wide_coarse_slabs():
+    """32 x 4 x 3 cubes: 32 fine slabs, 4 coarse slabs of 8."""
     from dynearthsol_gb300 import capi
     from dynearthsol_gb300.config import make_workload
     wl = make_workload("c1_3d_evp", cells=(32, 4, 3))
     per_call = _run(wl, capi.PREC_MIXED, 12)
-    assert _pipelined(per_call, 8), per_call
+    assert _pipelined(per_call, 4), per_call
 
 
 def test_permuted_mesh_takes_the_general_path():
