@@ -278,7 +278,11 @@ int des_step(des_ctx *ctx, int nsteps);
  * the fields that no step writes (coord0; stressyy outside plane strain) are
  * not downloaded: st ends as after upload + step + download, bit for bit,
  * with ~80 MB less host-link traffic at 1M tets.  Page-locked host arrays
- * let the copies run asynchronously at the link's rate. */
+ * let the copies run asynchronously at the link's rate.  With nsteps == 1,
+ * a complete page-locked state and a mesh numbered slab by slab (as the
+ * structured box meshes are), the upload, the step and the download overlap
+ * slab by slab (one CUDA graph, built on the first such call for these host
+ * arrays and reused while they stay the same). */
 int des_step_host(des_ctx *ctx, des_host_state *st, int nsteps);
 
 /* ---- output frames in the reference's .save format ---------------------
