@@ -89,3 +89,36 @@ def test_permuted_mesh_takes_the_general_path():
     wl = make_workload("c4_3d_heat_jitter", cells=(16, 4, 3))
     per_call = _run(wl, capi.PREC_MIXED, 3)
     assert max(per_call) < 33, per_call
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_pipelined_with_yielding(prec):
+    """The weakened, fast-loaded material of the yielding golden cases on a
+    16 x 4 x 3 box: the return map and the EVP branch choice run in the
+    slabs; plastic strain must appear."""
+    from cases import _fast, _weak
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import initial_state, make_workload
+    from dynearthsol_gb300.solver import DeviceModel
+    wl = make_workload("c1_3d_evp", cells=(16, 4, 3))
+    wl.params = _fast(wl.params)
+    wl.mat = _weak(wl.mat)
+    precision = capi.PREC_FP64 if prec == "fp64" else capi.PREC_MIXED
+    per_call = _run(wl, precision, 12)
+    assert _pipelined(per_call, 4), per_call
+    st0, cp = initial_state(wl)
+    m = DeviceModel(wl, comp_pressure=cp, precision=precision)
+    init = m.init_fields(st0)
+    m.upload(init, m.clock())
+    m.step(12)
+    assert np.count_nonzero(m.download()["plstrain"]) > 0
+
+
+def test_pipelined_2d():
+    """2D box of 32 x 4 rectangles (plane strain elasto-plastic): 32 fine
+    slabs of one column, 4 coarse slabs."""
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import make_workload
+    wl = make_workload("c0_2d_ep", cells=(32, 4))
+    per_call = _run(wl, capi.PREC_FP64, 12)
+    assert _pipelined(per_call, 4), per_call
