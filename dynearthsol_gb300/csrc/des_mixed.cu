@@ -79,25 +79,25 @@ __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *e
     return __hiloint2double(__double2hiint(m) + ((int)kf << 20), __double2loint(m));
 }
 
-// maxwell (rheology.cxx:118-134) with 1/viscosity and 1/(1+tmp) by
-// recip_newton instead of two FP64 divisions (f1, f2 then differ from the
-// FP64 step's by a few ulp), and the updates as fused multiply-adds.  The
-// divisions by 3 are div3, bit-identical.  Over 2000 steps of the
-// 998,400-tet workload with damping 2, these roundings leave the stress
-// within 8e-11 (relative L2) of the FP64 step's, the same as without the
-// fused forms.
+// maxwell (rheology.cxx:118-134).  The relaxation coefficients come from
+// FP32: tmp = dt G / (2 visc) and f2 - 1 = -tmp / (1 + tmp), each within
+// ~2^-22 of itself (the viscosity they scale is good to ~2e-7), so f1 =
+// 1 - tmp and f2 are one FP64 addition each instead of two FP64 Newton
+// reciprocals.  The updates are fused multiply-adds, and the mean stress
+// and K dv are added to the deviator in one step.  The divisions by 3 are
+// div3, bit-identical.
 __device__ __forceinline__ void maxwell_mixed(double bulkm, double shearm, double viscosity, double dt, double dv,
                                               const double *de, double *s)
 {
-    const double tmp = 0.5 * dt * shearm * recip_newton(viscosity);
-    const double f1 = 1 - tmp;
-    const double f2 = recip_newton(1 + tmp);
+    const float tf = (0.5f * f32_of(dt) * f32_of(shearm)) / f32_of(viscosity);
+    const double f1 = 1 - f64_of(tf);
+    const double f2 = 1 + f64_of(-tf / (1.0f + tf));
     const double dev = div3(de[0] + de[1] + de[2]);
     const double s0 = div3(s[0] + s[1] + s[2]);
     const double g2 = 2 * shearm;
-    const double kdv = bulkm * dv;
+    const double s0k = s0 + bulkm * dv;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) s[i] = fma(fma(s[i] - s0, f1, g2 * (de[i] - dev)), f2, s0) + kdv;
+    for (int i = 0; i < 3; ++i) s[i] = fma(fma(s[i] - s0, f1, g2 * (de[i] - dev)), f2, s0k);
 #pragma unroll
     for (int i = 3; i < 6; ++i) s[i] = fma(s[i], f1, g2 * de[i]) * f2;
 }
@@ -203,12 +203,18 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
             // the choice is rounding-decided in near-lithostatic elements of high
             // viscosity (J2 of a small deviator formed from pressure-sized
             // components), and the two candidates differ in pressure (K dv
-            // against K tr(de)): J2 is evaluated exactly as the FP64 step does
-            const double svII = second_invariant2_<3>(sv);
-            const double spII = screened   // sp is the trial stress: second_invariant2_<3>(sp), bit for bit
-                ? 0.5 * (q[0] * q[0] + q[1] * q[1] + q[2] * q[2]) + sp[3] * sp[3] + sp[4] * sp[4] + sp[5] * sp[5]
-                : second_invariant2_<3>(sp);
-            if (svII < spII) {
+            // against K tr(de)): J2 is evaluated exactly as the FP64 step does,
+            // unless the FP32 estimates already decide the comparison (their
+            // bounds cover the FP64 evaluation's rounding)
+            int vless = j2_less(j2_est3(sv), screened ? j2_est_dev3(q, sp) : j2_est3(sp));
+            if (vless < 0) {
+                const double svII = second_invariant2_<3>(sv);
+                const double spII = screened   // sp is the trial stress: second_invariant2_<3>(sp), bit for bit
+                    ? 0.5 * (q[0] * q[0] + q[1] * q[1] + q[2] * q[2]) + sp[3] * sp[3] + sp[4] * sp[4] + sp[5] * sp[5]
+                    : second_invariant2_<3>(sp);
+                vless = svII < spII;
+            }
+            if (vless) {
 #pragma unroll
                 for (int i = 0; i < 6; ++i) s[i] = sv[i];
             } else {

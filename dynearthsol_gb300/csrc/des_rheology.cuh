@@ -343,19 +343,26 @@ __device__ __forceinline__ void jacobi3f(const float d[6], float w[3], float (&v
 
 // Screen of the Mohr-Coulomb yield test (rheology.cxx:163-178) in FP32, for
 // 3D.  The deviatoric trial stress D is diagonalised in FP32 (eigenvalues
-// only); the principal stresses and yield functions are formed in FP64 from
-// the FP64 mean stress m.  Each computed eigenvalue lies within ||E||_2 of
-// the exact one (Weyl), E being the backward error of rounding D to FP32 and
-// of twelve Jacobi rotations: a few tens of eps32 ||D||_F.  The FP64
+// only).  Each computed eigenvalue lies within ||E||_2 of the exact one
+// (Weyl), E being the backward error of rounding D to FP32 and of twelve
+// Jacobi rotations: a few tens of eps32 ||D||_F.  The principal stresses
+// p = m + w and the yield functions fs = p0 - p2 anphi + amc, ft = p2 -
+// ten_max are formed in FP32 too, from the FP64 mean stress m and material
+// terms rounded to FP32: with P = |m| + ||D||, that adds at most
+// 2^-21.6 (1 + anphi) P to fs and 2^-22 (P + |ten_max|) to ft.  The FP64
 // principal stresses of the full stress (principal_stresses3) carry errors
-// of a few eps64 (|m| + ||D||).  The screen passes an element only when both
-// yield functions clear the surface by tol = 2^-12 ||D||_F + 2^-40 |m|
-// (~4000 eps32 ||D||_F plus ~200 times the FP64 error in |m|), plus 2^-100
-// for the conversions' flush of magnitudes below 2^-126 to zero, so a passed
-// element is elastic in the FP64 test too: its output is its trial stress,
-// bit for bit, and the eigen-solve is skipped.  Every other element takes
-// the FP64 return map, including the choice of principal directions when
-// two principal stresses (nearly) coincide, which FP32 cannot resolve.
+// of a few eps64 P.  The screen passes an element only when both yield
+// functions clear the surface by tol = 2^-12 ||D||_F + 2^-19 (|m| +
+// ||D||_F) (~4000 eps32 ||D||_F plus four times the FP32 arithmetic's
+// error), plus 2^-19 of the material term, plus 2^-100 for the conversions'
+// flush of magnitudes below 2^-126 to zero, so a passed element is elastic
+// in the FP64 test too: its output is its trial stress, bit for bit, and the
+// eigen-solve is skipped.  Every other element takes the FP64 return map,
+// including the choice of principal directions when two principal stresses
+// (nearly) coincide, which FP32 cannot resolve.  Elements within ~2^-19 |m|
+// of the yield surface fail the screen and take the return map; they are
+// few, and the result does not depend on it.  A non-finite conversion makes
+// a comparison false: such an element takes the return map.
 // The same screen given the mean stress m and the normal deviator q_i = s_i - m
 // (any FP64 rounding of m is covered by tol).
 __device__ __forceinline__ bool clearly_elastic3_dev(double amc, double anphi, double ten_max, double m,
@@ -366,11 +373,12 @@ __device__ __forceinline__ bool clearly_elastic3_dev(double amc, double anphi, d
     jacobi3f(d, w, v);
     const float nf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
                            + 2.0f * (d[3] * d[3] + d[4] * d[4] + d[5] * d[5]));
-    const double tol = f64_of(nf) * (1.0 / 4096) + 0x1p-40 * fabs(m) + 0x1p-100;
-    const double p0 = m + f64_of(w[0]), p2 = m + f64_of(w[2]);
-    const double fs = p0 - p2 * anphi + amc;
-    const double ft = p2 - ten_max;
-    return fs > (1 + anphi) * tol && ft < -tol;
+    const float mf = f32_of(m), af = f32_of(anphi), cf = f32_of(amc), tf = f32_of(ten_max);
+    const float tol = 0x1p-12f * nf + 0x1p-19f * (fabsf(mf) + nf) + 0x1p-100f;
+    const float p0 = mf + w[0], p2 = mf + w[2];
+    const float fs = p0 - p2 * af + cf;
+    const float ft = p2 - tf;
+    return fs > (1.0f + af) * tol + 0x1p-19f * fabsf(cf) && ft < -(tol + 0x1p-19f * fabsf(tf));
 }
 
 __device__ __forceinline__ bool clearly_elastic3(double amc, double anphi, double ten_max, const double *s)
@@ -378,6 +386,60 @@ __device__ __forceinline__ bool clearly_elastic3(double amc, double anphi, doubl
     const double m = (s[0] + s[1] + s[2]) * (1.0 / 3);
     const double q[3] = {s[0] - m, s[1] - m, s[2] - m};
     return clearly_elastic3_dev(amc, anphi, ten_max, m, q, s);
+}
+
+// The EVP branch choice (rheology.cxx:594-634) compares second_invariant2_
+// (utils.hpp:110-128) of two candidate stresses.  J2Est is an FP32 estimate
+// j of that FP64 value with a bound tol on their distance; j2_less decides
+// the comparison from two estimates where they are further apart than both
+// bounds together, and otherwise leaves it to the FP64 evaluation.
+struct J2Est {
+    float j, tol;
+};
+
+// Estimate of second_invariant2_<3>(s).  Let u = 2^-53, S = max |s_i| over
+// the normal components and J* the exact J2 of s.  The normal deviator
+// enters through the FP64 pairwise differences s_i - s_j, each within u of
+// itself: 0.5 sum_i (s_i - mean)^2 = (1/6) sum_{i<j} (s_i - s_j)^2, so no
+// pressure cancels in FP32.  The FP32 evaluation (conversions, squares,
+// sums, the constant 1/6) then lies within 9 * 2^-24 J* of J*.
+// second_invariant2_'s mean lies within 2.7 u S of the exact mean and each
+// of its deviator components within 5 u S of the exact one, which moves its
+// J2 by at most 5 sqrt(6) u S sqrt(J*) + 37.5 u^2 S^2; its twelve roundings
+// of nonnegative terms add at most 12 u J*.  tol = 2^-19 j + 2^-48 S
+// sqrt(j) + (2^-50 S)^2 + 2^-100 covers these terms by factors of 1.7 and
+// more, with its own FP32 rounding and the conversions' flush of magnitudes
+// below 2^-126 to zero.  An infinite or NaN estimate gives an infinite or
+// NaN tol, which decides nothing.
+__device__ __forceinline__ J2Est j2_est3(const double *s)
+{
+    const float d01 = f32_of(s[0] - s[1]), d02 = f32_of(s[0] - s[2]), d12 = f32_of(s[1] - s[2]);
+    const float t3 = f32_of(s[3]), t4 = f32_of(s[4]), t5 = f32_of(s[5]);
+    const float j = (d01 * d01 + d02 * d02 + d12 * d12) * (1.0f / 6) + (t3 * t3 + t4 * t4 + t5 * t5);
+    const float S = fmaxf(fmaxf(fabsf(f32_of(s[0])), fabsf(f32_of(s[1]))), fabsf(f32_of(s[2])));
+    const float h = 0x1p-50f * S;
+    return {j, 0x1p-19f * j + 0x1p-48f * S * sqrtf(j) + h * h + 0x1p-100f};
+}
+
+// Estimate of 0.5 (q0^2 + q1^2 + q2^2) + s3^2 + s4^2 + s5^2 evaluated in
+// FP64 on these very q_i (a deviator formed as second_invariant2_ forms it)
+// and shear components: the FP32 evaluation lies within 7 * 2^-24 of the
+// exact value of the expression, the FP64 one within 12 u; tol = 2^-19 j +
+// 2^-100 covers both and the flush below 2^-126.
+__device__ __forceinline__ J2Est j2_est_dev3(const double *q, const double *s)
+{
+    const float q0 = f32_of(q[0]), q1 = f32_of(q[1]), q2 = f32_of(q[2]);
+    const float t3 = f32_of(s[3]), t4 = f32_of(s[4]), t5 = f32_of(s[5]);
+    const float j = 0.5f * (q0 * q0 + q1 * q1 + q2 * q2) + (t3 * t3 + t4 * t4 + t5 * t5);
+    return {j, 0x1p-19f * j + 0x1p-100f};
+}
+
+// 1 when the FP64 J2 behind a is certainly below that behind b, 0 when it
+// certainly is not (equal included), -1 when the estimates are too close
+__device__ __forceinline__ int j2_less(const J2Est &a, const J2Est &b)
+{
+    const float gap = b.j - a.j, tol = a.tol + b.tol;
+    return gap > tol ? 1 : (-gap > tol ? 0 : -1);
 }
 
 // Mohr-Coulomb return map in principal space of the elastic trial stress s
@@ -593,7 +655,6 @@ __device__ unsigned update_stress_elem(const KP &p, int e, double dt, double *s,
 #pragma unroll
         for (int i = 0; i < NSTR; ++i) sv[i] = s[i];
         maxwell_<ND>(bulkm, shearm, viscosity, dt, dv, de, sv);
-        double svII = second_invariant2_<ND>(sv);
         double amc, anphi, anpsi, hardn, ten_max;
         m_plastic_props(p, e, pls, amc, anphi, anpsi, hardn, ten_max);
         double sp[NSTR], spyy = syy;
@@ -603,9 +664,12 @@ __device__ unsigned update_stress_elem(const KP &p, int e, double dt, double *s,
             elasto_plastic2d_(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, sp, spyy);
         else if (elasto_plastic_<ND>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, sp))
             bits |= DES_DEV_QL_NOCONV;
-        double spII = second_invariant2_<ND>(sp);
-        if (p.tape_evp) p.tape_evp[e] = svII < spII ? 0 : 1;
-        if (svII < spII) {
+        // svII < spII, decided in FP32 where the two are clearly apart
+        int vless = -1;
+        if constexpr (ND == 3) vless = j2_less(j2_est3(sv), j2_est3(sp));
+        if (vless < 0) vless = second_invariant2_<ND>(sv) < second_invariant2_<ND>(sp);
+        if (p.tape_evp) p.tape_evp[e] = vless ? 0 : 1;
+        if (vless) {
 #pragma unroll
             for (int i = 0; i < NSTR; ++i) s[i] = sv[i];
         } else {
