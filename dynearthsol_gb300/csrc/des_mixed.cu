@@ -86,20 +86,40 @@ __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *e
 // reciprocals.  The updates are fused multiply-adds, and the mean stress
 // and K dv are added to the deviator in one step.  The divisions by 3 are
 // div3, bit-identical.
+struct MaxwellCoef {
+    double f1, f2;
+};
+
+__device__ __forceinline__ MaxwellCoef maxwell_coef(double shearm, double viscosity, double dt)
+{
+    const float tf = (0.5f * f32_of(dt) * f32_of(shearm)) / f32_of(viscosity);
+    return {1 - f64_of(tf), 1 + f64_of(-tf / (1.0f + tf))};
+}
+
+// the update on the old normal deviator x_i = s_i - s0 and y_i = 2G (de_i -
+// tr(de)/3); s0k = s0 + K dv; s and de for the shear components
+__device__ __forceinline__ void maxwell_mixed_xy(const MaxwellCoef &c, double g2, double s0k, const double *x,
+                                                 const double *y, const double *s, const double *de, double *out)
+{
+#pragma unroll
+    for (int i = 0; i < 3; ++i) out[i] = fma(fma(x[i], c.f1, y[i]), c.f2, s0k);
+#pragma unroll
+    for (int i = 3; i < 6; ++i) out[i] = fma(s[i], c.f1, g2 * de[i]) * c.f2;
+}
+
 __device__ __forceinline__ void maxwell_mixed(double bulkm, double shearm, double viscosity, double dt, double dv,
                                               const double *de, double *s)
 {
-    const float tf = (0.5f * f32_of(dt) * f32_of(shearm)) / f32_of(viscosity);
-    const double f1 = 1 - f64_of(tf);
-    const double f2 = 1 + f64_of(-tf / (1.0f + tf));
     const double dev = div3(de[0] + de[1] + de[2]);
     const double s0 = div3(s[0] + s[1] + s[2]);
     const double g2 = 2 * shearm;
-    const double s0k = s0 + bulkm * dv;
+    double x[3], y[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) s[i] = fma(fma(s[i] - s0, f1, g2 * (de[i] - dev)), f2, s0k);
-#pragma unroll
-    for (int i = 3; i < 6; ++i) s[i] = fma(s[i], f1, g2 * de[i]) * f2;
+    for (int i = 0; i < 3; ++i) {
+        x[i] = s[i] - s0;
+        y[i] = g2 * (de[i] - dev);
+    }
+    maxwell_mixed_xy(maxwell_coef(shearm, viscosity, dt), g2, s0 + bulkm * dv, x, y, s, de, s);
 }
 
 // elastic_ (rheology.cxx:13-40) with fused multiply-adds: 2G de_i + lambda tr(de)
@@ -174,55 +194,85 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
         viscous_<3>(bulkm, visc_mixed(p, e, edot, T), es[0] + es[1] + es[2], edot, s);
     } else if (rt == DES_RH_MAXWELL) {
         maxwell_mixed(bulkm, shearm, visc_mixed(p, e, edot, T), dt, dvol_mixed(p, e), de, s);
-    } else {
+    } else if (rt == DES_RH_EP) {
         double amc, anphi, anpsi, hardn, ten_max;
         m_plastic_props(p, e, pls, amc, anphi, anpsi, hardn, ten_max);
-        double sp[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) sp[i] = s[i];
-        elastic_mixed(bulkm, shearm, de, sp);
-        // mean and normal deviator of the trial stress, as second_invariant2_
-        // forms them: shared by the yield screen and, for a screened element,
-        // by J2 of the EVP choice
-        const double am = div3(sp[0] + sp[1] + sp[2]);
-        const double q[3] = {sp[0] - am, sp[1] - am, sp[2] - am};
+        elastic_mixed(bulkm, shearm, de, s);
+        const double am = div3(s[0] + s[1] + s[2]);
+        const double q[3] = {s[0] - am, s[1] - am, s[2] - am};
         double depls = 0;
-        const bool screened = clearly_elastic3_dev(amc, anphi, ten_max, am, q, sp);
-        if (!screened && mc_return_<3>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp))
+        if (!clearly_elastic3_dev(amc, anphi, ten_max, am, q, s)
+            && mc_return_<3>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, s))
             bits |= DES_DEV_QL_NOCONV;
-        if (rt == DES_RH_EP) {
+        pls += depls;
+        dpls = depls;
+    } else {   // EVP: the smaller second invariant wins (rheology.cxx:594-634)
+        double amc, anphi, anpsi, hardn, ten_max;
+        m_plastic_props(p, e, pls, amc, anphi, anpsi, hardn, ten_max);
+        // The two candidates share the old normal deviator x_i = s_i - s0
+        // and y_i = 2G (de_i - tr(de)/3).  The elastic trial stress has the
+        // deviator x + y up to roundings: with u = 2^-53 and S = |s0| +
+        // sum |x_i| + sum |y_i| + (2G + 2K) sum |de_i| (normal components),
+        // qt = x + y lies within 22 u S of the exact deviator of the FP64
+        // trial stress that elastic_mixed forms, and s0 + K tr(de) within
+        // 12 u S of its mean.  The yield screen and the J2 estimate run on qt,
+        // with that distance added to their bounds, so the FP64 trial stress
+        // is formed only for an element that they leave undecided or that
+        // the elasto-plastic candidate wins.  The Maxwell update uses the
+        // same x and y.
+        const double trde = de[0] + de[1] + de[2];
+        const double s0 = div3(old_s);
+        const double dev = div3(trde);
+        const double g2 = 2 * shearm;
+        double x[3], y[3], qt[3], sh[3];
 #pragma unroll
-            for (int i = 0; i < 6; ++i) s[i] = sp[i];
-            pls += depls;
-            dpls = depls;
-        } else {   // EVP: the smaller second invariant wins (rheology.cxx:594-634)
-            double sv[6];
+        for (int i = 0; i < 3; ++i) {
+            x[i] = s[i] - s0;
+            y[i] = g2 * (de[i] - dev);
+            qt[i] = x[i] + y[i];
+            sh[i] = fma(g2, de[i + 3], s[i + 3]);   // the trial's shear components, as elastic_mixed forms them
+        }
+        double sv[6];
+        maxwell_mixed_xy(maxwell_coef(shearm, visc_mixed(p, e, edot, T), dt), g2, s0 + bulkm * dvol_mixed(p, e), x,
+                         y, s, de, sv);
+        const float s0f = f32_of(s0), kf = f32_of(bulkm), ktr = kf * f32_of(trde);
+        float S = fabsf(s0f), sde = 0;
 #pragma unroll
-            for (int i = 0; i < 6; ++i) sv[i] = s[i];
-            maxwell_mixed(bulkm, shearm, visc_mixed(p, e, edot, T), dt, dvol_mixed(p, e), de, sv);
-            // the choice is rounding-decided in near-lithostatic elements of high
-            // viscosity (J2 of a small deviator formed from pressure-sized
+        for (int i = 0; i < 3; ++i) {
+            S += fabsf(f32_of(x[i])) + fabsf(f32_of(y[i]));
+            sde += fabsf(f32_of(de[i]));
+        }
+        S += 2.0f * (f32_of(g2) + fabsf(kf)) * sde;
+        const float d[6] = {f32_of(qt[0]), f32_of(qt[1]), f32_of(qt[2]), f32_of(sh[0]), f32_of(sh[1]), f32_of(sh[2])};
+        // dev_err: sqrt(3) 22 u S < 2^-46.7 S, taken as 2^-44 S
+        const bool elastic = clearly_elastic3_f(f32_of(anphi), f32_of(amc), f32_of(ten_max), s0f + ktr,
+                                                fabsf(s0f) + fabsf(ktr), d, 0x1p-44f * S);
+        int vless = elastic ? j2_less(j2_est3(sv), j2_est_near3(qt, sh, S)) : -1;
+        if (vless != 1) {
+            // the elasto-plastic candidate, exactly as the EP branch forms it
+            double sp[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) sp[i] = s[i];
+            elastic_mixed(bulkm, shearm, de, sp);
+            double depls = 0;
+            if (!elastic && mc_return_<3>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp))
+                bits |= DES_DEV_QL_NOCONV;
+            // the choice is rounding-decided in near-lithostatic elements of
+            // high viscosity (J2 of a small deviator formed from pressure-sized
             // components), and the two candidates differ in pressure (K dv
-            // against K tr(de)): J2 is evaluated exactly as the FP64 step does,
-            // unless the FP32 estimates already decide the comparison (their
-            // bounds cover the FP64 evaluation's rounding)
-            int vless = j2_less(j2_est3(sv), screened ? j2_est_dev3(q, sp) : j2_est3(sp));
-            if (vless < 0) {
-                const double svII = second_invariant2_<3>(sv);
-                const double spII = screened   // sp is the trial stress: second_invariant2_<3>(sp), bit for bit
-                    ? 0.5 * (q[0] * q[0] + q[1] * q[1] + q[2] * q[2]) + sp[3] * sp[3] + sp[4] * sp[4] + sp[5] * sp[5]
-                    : second_invariant2_<3>(sp);
-                vless = svII < spII;
-            }
-            if (vless) {
-#pragma unroll
-                for (int i = 0; i < 6; ++i) s[i] = sv[i];
-            } else {
+            // against K tr(de)): where the estimates leave it open, J2 is
+            // evaluated exactly as the FP64 step does
+            if (vless < 0) vless = second_invariant2_<3>(sv) < second_invariant2_<3>(sp);
+            if (!vless) {
 #pragma unroll
                 for (int i = 0; i < 6; ++i) s[i] = sp[i];
                 pls += depls;
                 dpls = depls;
             }
+        }
+        if (vless) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) s[i] = sv[i];
         }
     }
 #pragma unroll

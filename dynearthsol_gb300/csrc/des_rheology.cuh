@@ -363,22 +363,32 @@ __device__ __forceinline__ void jacobi3f(const float d[6], float w[3], float (&v
 // of the yield surface fail the screen and take the return map; they are
 // few, and the result does not depend on it.  A non-finite conversion makes
 // a comparison false: such an element takes the return map.
+// The screen on FP32 inputs: d the deviator (normal, then shear components),
+// mf the mean stress, mag an FP32 bound on |m| that also covers the FP32
+// rounding mf carries, dev_err a bound on the 2-norm distance of d (before
+// its rounding to FP32) from the exact deviator of the FP64 stress.
+__device__ __forceinline__ bool clearly_elastic3_f(float af, float cf, float tf, float mf, float mag,
+                                                   const float d[6], float dev_err)
+{
+    float w[3], v[3][3];
+    jacobi3f(d, w, v);
+    const float nf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
+                           + 2.0f * (d[3] * d[3] + d[4] * d[4] + d[5] * d[5]));
+    const float tol = 0x1p-12f * nf + 0x1p-19f * (mag + nf) + dev_err + 0x1p-100f;
+    const float p0 = mf + w[0], p2 = mf + w[2];
+    const float fs = p0 - p2 * af + cf;
+    const float ft = p2 - tf;
+    return fs > (1.0f + af) * tol + 0x1p-19f * fabsf(cf) && ft < -(tol + 0x1p-19f * fabsf(tf));
+}
+
 // The same screen given the mean stress m and the normal deviator q_i = s_i - m
 // (any FP64 rounding of m is covered by tol).
 __device__ __forceinline__ bool clearly_elastic3_dev(double amc, double anphi, double ten_max, double m,
                                                      const double *q, const double *s)
 {
     const float d[6] = {f32_of(q[0]), f32_of(q[1]), f32_of(q[2]), f32_of(s[3]), f32_of(s[4]), f32_of(s[5])};
-    float w[3], v[3][3];
-    jacobi3f(d, w, v);
-    const float nf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
-                           + 2.0f * (d[3] * d[3] + d[4] * d[4] + d[5] * d[5]));
-    const float mf = f32_of(m), af = f32_of(anphi), cf = f32_of(amc), tf = f32_of(ten_max);
-    const float tol = 0x1p-12f * nf + 0x1p-19f * (fabsf(mf) + nf) + 0x1p-100f;
-    const float p0 = mf + w[0], p2 = mf + w[2];
-    const float fs = p0 - p2 * af + cf;
-    const float ft = p2 - tf;
-    return fs > (1.0f + af) * tol + 0x1p-19f * fabsf(cf) && ft < -(tol + 0x1p-19f * fabsf(tf));
+    const float mf = f32_of(m);
+    return clearly_elastic3_f(f32_of(anphi), f32_of(amc), f32_of(ten_max), mf, fabsf(mf), d, 0.0f);
 }
 
 __device__ __forceinline__ bool clearly_elastic3(double amc, double anphi, double ten_max, const double *s)
@@ -432,6 +442,23 @@ __device__ __forceinline__ J2Est j2_est_dev3(const double *q, const double *s)
     const float t3 = f32_of(s[3]), t4 = f32_of(s[4]), t5 = f32_of(s[5]);
     const float j = 0.5f * (q0 * q0 + q1 * q1 + q2 * q2) + (t3 * t3 + t4 * t4 + t5 * t5);
     return {j, 0x1p-19f * j + 0x1p-100f};
+}
+
+// Estimate of second_invariant2_<3> of an FP64 stress s from a normal
+// deviator qt that lies within 22 u S of the exact deviator of s in each
+// component, and from the shear components of s itself (S an FP32 bound on
+// the magnitudes behind both).  Against the exact J2 of s, J*, the FP32
+// evaluation on qt is off by at most 7 * 2^-24 J + sqrt(6) 22 u S sqrt(J*)
+// + 1.5 (22 u S)^2; second_invariant2_ by 12 u J* + 12.25 u S sqrt(J*) +
+// 37.5 u^2 S^2 (j2_est3).  tol = 2^-19 j + 2^-44 S sqrt(j) + (2^-46 S)^2 +
+// 2^-100 covers the sum by factors of 3.7 and more.
+__device__ __forceinline__ J2Est j2_est_near3(const double *qt, const double *sh, float S)
+{
+    const float q0 = f32_of(qt[0]), q1 = f32_of(qt[1]), q2 = f32_of(qt[2]);
+    const float t3 = f32_of(sh[0]), t4 = f32_of(sh[1]), t5 = f32_of(sh[2]);
+    const float j = 0.5f * (q0 * q0 + q1 * q1 + q2 * q2) + (t3 * t3 + t4 * t4 + t5 * t5);
+    const float h = 0x1p-46f * S;
+    return {j, 0x1p-19f * j + 0x1p-44f * S * sqrtf(j) + h * h + 0x1p-100f};
 }
 
 // 1 when the FP64 J2 behind a is certainly below that behind b, 0 when it
