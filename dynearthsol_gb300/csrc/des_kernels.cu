@@ -569,8 +569,10 @@ __device__ __forceinline__ double cof(double a, double b, double c, double d)
     return C ? fma(a, b, -(c * d)) : a * b - c * d;
 }
 
-// FAST_RECIP: the mixed step's form, 1/(6 vol) by recip_newton and the
-// cofactors with fused multiply-adds (an ulp from the FP64 step's values)
+// FAST_RECIP: the mixed step's form, 1/(6 vol) by recip_newton, the
+// cofactors with fused multiply-adds (an ulp from the FP64 step's values),
+// and the first node's derivatives as minus the sum of the other three
+// (the four sum to zero: the element's nodal forces then balance)
 template <int ND, bool FAST_RECIP = false>
 __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], const TetEdges &te, double vol,
                                               double (*shp)[ND + 1])
@@ -580,18 +582,24 @@ __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], const TetEd
         const double x01 = te.x01, x02 = te.x02, x03 = te.x03, x12 = te.x12, x13 = te.x13, x23 = te.x23;
         const double y01 = te.y01, y02 = te.y02, y03 = te.y03, y12 = te.y12, y13 = te.y13, y23 = te.y23;
         const double z01 = te.z01, z02 = te.z02, z03 = te.z03, z12 = te.z12, z13 = te.z13, z23 = te.z23;
-        shp[0][0] = iv * cof<FAST_RECIP>(y13, z12, y12, z13);
+        if (!FAST_RECIP) {
+            shp[0][0] = iv * cof<FAST_RECIP>(y13, z12, y12, z13);
+            shp[1][0] = iv * cof<FAST_RECIP>(z13, x12, z12, x13);
+            shp[ND - 1][0] = iv * cof<FAST_RECIP>(x13, y12, x12, y13);
+        }
         shp[0][1] = iv * cof<FAST_RECIP>(y02, z23, y23, z02);
         shp[0][2] = iv * cof<FAST_RECIP>(y13, z03, y03, z13);
         shp[0][3] = iv * cof<FAST_RECIP>(y01, z02, y02, z01);
-        shp[1][0] = iv * cof<FAST_RECIP>(z13, x12, z12, x13);
         shp[1][1] = iv * cof<FAST_RECIP>(z02, x23, z23, x02);
         shp[1][2] = iv * cof<FAST_RECIP>(z13, x03, z03, x13);
         shp[1][3] = iv * cof<FAST_RECIP>(z01, x02, z02, x01);
-        shp[ND - 1][0] = iv * cof<FAST_RECIP>(x13, y12, x12, y13);
         shp[ND - 1][1] = iv * cof<FAST_RECIP>(x02, y23, x23, y02);
         shp[ND - 1][2] = iv * cof<FAST_RECIP>(x13, y03, x03, y13);
         shp[ND - 1][3] = iv * cof<FAST_RECIP>(x01, y02, x02, y01);
+        if (FAST_RECIP) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) shp[k][0] = -((shp[k][1] + shp[k][2]) + shp[k][3]);
+        }
     } else {
         const double *d0 = d[0], *d1 = d[1], *d2 = d[2];
         double iv = FAST_RECIP ? recip_newton(2 * vol) : 1 / (2 * vol);
@@ -692,16 +700,21 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
                 for (int i = 0; i < NPE; ++i) shp[k][i] = p.shp[((size_t)k * NPE + i) * ne + e];
         }
         if ((flags & GEO_ROTATE) && ND == 3 && p.shp32) {
-            // mixed step: spin from FP64 velocity differences, FP32 Jaumann
-            // increments added to the FP64 stress and strain
+            // mixed step: spin from FP32 velocity differences, FP32 Jaumann
+            // increments added to the FP64 stress and strain.  Rounding the
+            // velocities to FP32 moves a difference by ~2^-23 |v|: against
+            // differences ~|v| h / L across an element of size h in a field
+            // varying over L, a relative error ~2^-23 L / h in the spin,
+            // whose increment dt W s is itself ~1e-8 of the stress per step.
             double v0[ND];
             load_node_v<ND>(p, nodes[0], v0);
+            const float v00 = f32_of(v0[0]), v01 = f32_of(v0[1]), v02 = f32_of(v0[ND - 1]);
             float w3 = 0, w4 = 0, w5 = 0;
 #pragma unroll
             for (int i = 1; i < NPE; ++i) {
                 double vi[ND];
                 load_node_v<ND>(p, nodes[i], vi);
-                const float d0 = f32_of(vi[0] - v0[0]), d1 = f32_of(vi[1] - v0[1]), d2 = f32_of(vi[ND - 1] - v0[ND - 1]);
+                const float d0 = f32_of(vi[0]) - v00, d1 = f32_of(vi[1]) - v01, d2 = f32_of(vi[ND - 1]) - v02;
                 const float sx = f32_of(shp[0][i]), sy = f32_of(shp[1][i]), sz = f32_of(shp[ND - 1][i]);
                 w3 += 0.5f * (d0 * sy - d1 * sx);
                 w4 += 0.5f * (d0 * sz - d2 * sx);
@@ -714,10 +727,12 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
                 double S[6];
 #pragma unroll
                 for (int cc = 0; cc < 6; ++cc) S[cc] = arr[a][cc * ne + e];
-                // the isotropic part does not rotate: the normal-stress
-                // differences are taken in FP64, so the pressure never
-                // enters the FP32 products
-                const float d01 = f32_of(S[0] - S[1]), d02 = f32_of(S[0] - S[2]), d12 = f32_of(S[1] - S[2]);
+                // the isotropic part does not rotate: only normal-stress
+                // differences enter.  Taken in FP32, each is off by ~2^-23
+                // |S|, which the increment scales by dt |W| (~1e-8): ~1e-15
+                // of the stress per step, of random sign
+                const float S0 = f32_of(S[0]), S1 = f32_of(S[1]), S2 = f32_of(S[2]);
+                const float d01 = S0 - S1, d02 = S0 - S2, d12 = S1 - S2;
                 const float f3 = f32_of(S[3]), f4 = f32_of(S[4]), f5 = f32_of(S[5]);
                 float si[6];
                 si[0] = -2.0f * f3 * w3 - 2.0f * f4 * w4;
