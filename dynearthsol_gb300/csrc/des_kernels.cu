@@ -342,7 +342,7 @@ __device__ void facet_force(const KP &p, int q)
             normal[0] = (v01[1] * v02[2] - v01[2] * v02[1]) / 2;
             normal[1] = (v01[2] * v02[0] - v01[0] * v02[2]) / 2;
             normal[ND - 1] = (v01[0] * v02[1] - v01[1] * v02[0]) / 2;
-            zcenter = (c0[2] + c1[2] + c2[2]) / 3;
+            zcenter = div3(c0[2] + c1[2] + c2[2]);   // x / 3, bit for bit
         } else {
             const int F[3][2] = {{1, 2}, {2, 0}, {0, 1}};
             double c0[2], c1[2];
@@ -369,7 +369,7 @@ __device__ void facet_force(const KP &p, int q)
             pr = ref_pressure_(p, zcenter);
         }
 #pragma unroll
-        for (int d = 0; d < ND; ++d) out[d] = pr * normal[d] / ND;
+        for (int d = 0; d < ND; ++d) out[d] = divnd<ND>(pr * normal[d]);
     }
 #pragma unroll
     for (int d = 0; d < ND; ++d) p.fv[(size_t)d * p.nbf + q] = out[d];
