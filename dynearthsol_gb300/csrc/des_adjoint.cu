@@ -7,7 +7,10 @@
 // derivative of the branch the forward took: a subgradient at the kinks.
 // Where the forward's map is discontinuous in its input -- the eigenbasis
 // of repeated principal stresses, the sign of a zero force under damping --
-// the term of the discontinuity is dropped.
+// the term of the discontinuity is dropped.  Adjoints are checked against
+// finite differences, not bit for bit: divisions by 3 are div3, and the
+// reciprocals of the common paths are recip_newton (~1e-14 relative), each
+// a few FP64 instructions instead of an FP64 division.
 #include <cfloat>
 
 #include "des_adjoint.cuh"
@@ -50,7 +53,7 @@ __device__ void geom_reverse(const double (*c)[3], double vol, const double (*gs
 {
     const int PA[4][2] = {{1, 3}, {0, 2}, {1, 3}, {0, 1}};
     const int PB[4][2] = {{1, 2}, {2, 3}, {0, 3}, {0, 2}};
-    const double iv = 1 / (6 * vol);
+    const double iv = recip_newton(6 * vol);
     double giv = 0;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -74,9 +77,9 @@ __device__ void geom_reverse(const double (*c)[3], double vol, const double (*gs
             gc[a1][Q] += gt * Pb;
         }
     }
-    gvol += giv * (-iv / vol);
+    gvol += giv * (-6 * iv * iv);   // d/dvol 1/(6 vol) = -6 iv^2
     // V = [x01 (y23 z12 - y12 z23) + x12 (y01 z23 - y23 z01) + x23 (y12 z01 - y01 z12)] / 6
-    const double g6 = gvol / 6;
+    const double g6 = div6(gvol);
     const double x01 = c[0][0] - c[1][0], x12 = c[1][0] - c[2][0], x23 = c[2][0] - c[3][0];
     const double y01 = c[0][1] - c[1][1], y12 = c[1][1] - c[2][1], y23 = c[2][1] - c[3][1];
     const double z01 = c[0][2] - c[1][2], z12 = c[1][2] - c[2][2], z23 = c[2][2] - c[3][2];
@@ -296,14 +299,14 @@ __global__ void __launch_bounds__(TPB_A) k_adj_motion(KP p, AdjBufs a, TapeStep 
                 gva[ib] = col[0] * gv[0] + col[1] * gv[1] + col[2] * gv[2];
             }
         }
-        const double m = t.mass[n];
+        const double im = recip_newton(t.mass[n]);
         double gm = 0, gf[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const double f = t.f[d * nn + n];
             a.av[d * nn + n] = gpre[d];
-            gf[d] = dt * gpre[d] / m;
-            gm -= gf[d] * f / m;
+            gf[d] = dt * gpre[d] * im;
+            gm -= gf[d] * f * im;
             double dd = 1;
             if (p.prm.is_quasi_static) dd = damp_deriv(p, f, t.v[d * nn + n]);
             gf[d] *= dd;
@@ -395,8 +398,8 @@ __global__ void __launch_bounds__(TPB_A) k_adj_facets(KP p, AdjBufs a, TapeStep 
         double gpr = 0, gn[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            gpr += gfv[d] * nrm[d] / 3;
-            gn[d] = gfv[d] * pr / 3;
+            gpr += div3(gfv[d] * nrm[d]);
+            gn[d] = div3(gfv[d] * pr);
         }
         grho = gpr * grho_per_gpr;
         const double gzc = gpr * gzc_per_gpr;
@@ -411,7 +414,7 @@ __global__ void __launch_bounds__(TPB_A) k_adj_facets(KP p, AdjBufs a, TapeStep 
             gc[2][d] = gb[d];
         }
 #pragma unroll
-        for (int j = 0; j < 3; ++j) gc[j][2] += gzc / 3;
+        for (int j = 0; j < 3; ++j) gc[j][2] += div3(gzc);
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -491,9 +494,9 @@ __global__ void __launch_bounds__(TPB_A) k_adj_nmd_nodes(KP p, AdjBufs a, TapeSt
     const size_t nn = p.nn, nbf = p.nbf;
     double acc = 0;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) acc += a.slot1[p.sup_ent[q] >> 2];
-    const double vn = t.voln[n];
-    a.adpn[n] = acc / vn;
-    a.avn[n] -= acc * t.dpn[n] / vn;
+    const double ivn = recip_newton(t.voln[n]);
+    a.adpn[n] = acc * ivn;
+    a.avn[n] -= acc * t.dpn[n] * ivn;
     if (p.nf_off[n] < p.nf_off[n + 1]) {
         const int F[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
         double gx[3] = {0, 0, 0};
@@ -560,9 +563,9 @@ __device__ __forceinline__ void maxwell_reverse(double K, double G, double visc,
                                                 const double *s, const double *go, double *gs, double *gde,
                                                 double &gG, double &gvisc, double &gdv)
 {
-    const double ivisc = 1 / visc;
+    const double ivisc = recip_newton(visc);
     const double tmp = 0.5 * dt * G * ivisc;
-    const double f1 = 1 - tmp, f2 = 1 / (1 + tmp);
+    const double f1 = 1 - tmp, f2 = recip_newton(1 + tmp);
     const double dev = div3(de[0] + de[1] + de[2]), s0 = div3(s[0] + s[1] + s[2]);
     double gf1 = 0, gf2 = 0, gs0 = 0, gdev = 0;
 #pragma unroll
@@ -590,8 +593,8 @@ __device__ __forceinline__ void maxwell_reverse(double K, double G, double visc,
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        gs[i] += gs0 / 3;
-        gde[i] += gdev / 3;
+        gs[i] += div3(gs0);
+        gde[i] += div3(gdev);
     }
     const double gtmp = -gf1 - gf2 * f2 * f2;
     gG += gtmp * 0.5 * dt * ivisc;
@@ -628,11 +631,13 @@ __device__ void visc_reverse(const KP &p, int e, const double *edot, double T, d
     }
     const double gas_constant = 8.3144;
     const double q = p.mat.visc_activation_energy[0] / (p.mat.visc_exponent[0] * gas_constant);
-    gT += gvisc * raw * (-q / (T * T));
+    const double iT = recip_newton(T);
+    gT -= gvisc * raw * q * iT * iT;
     if (ed < 0) ed = dmax_(second_invariant_<3>(edot), 1e-30);   // as visc_eval forms it
     if (ed > 1e-30) {
-        const double ged = gvisc * raw * p.mat.visc_pw[0] / ed;
-        const double gj2 = ged / (2 * ed);
+        const double ied = recip_newton(ed);
+        const double ged = gvisc * raw * p.mat.visc_pw[0] * ied;
+        const double gj2 = 0.5 * ged * ied;
         const double a = div3(edot[0] + edot[1] + edot[2]);
 #pragma unroll
         for (int i = 0; i < 3; ++i) gedot[i] += gj2 * (edot[i] - a);
@@ -928,7 +933,7 @@ __global__ void __launch_bounds__(TPB_A) k_adj_stress(KP p, AdjBufs a, TapeStep 
     if (viscous && gvisc != 0) visc_reverse(p, e, edot, T, raw, ed, gvisc, gec, gT, glv);
 #pragma unroll
     for (int cc = 0; cc < 6; ++cc) gec[cc] += dt * gde[cc];
-    const double ivo = 1 / volo;
+    const double ivo = recip_newton(volo);
     gvol += gdv * ivo;
     gvolo -= gdv * vol * ivo * ivo;
     // corrected strain rate -> strain rate before the correction, edvoldt
