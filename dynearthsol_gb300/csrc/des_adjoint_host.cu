@@ -4,8 +4,14 @@
 //
 // Memory: a checkpoint holds the state and its derived fields (~180 B per
 // tet); the tape of one segment holds checkpoint_every + 1 step records
-// (~360 B per tet each, the forward values the reverse kernels read).  At
+// (~367 B per tet each, the forward values the reverse kernels read).  At
 // 1M tets and 50 steps per segment that is ~18 GB of HBM.
+//
+// A window of one segment (checkpoint_every >= nsteps) is taped by the
+// forward itself: it writes each step's record as it goes, and the backward
+// runs the reverse kernels alone, with no recompute.  It needs the same
+// tape as the backward of a one-segment window would: 500 steps of the
+// 998,400-tet case are ~184 GB, which GB300's HBM holds.
 #include <algorithm>
 #include <vector>
 
@@ -101,6 +107,7 @@ struct AdjWork {
     int K = 0, C = 0, nseg = 0;
     double dt = 0;
     bool recorded = false;
+    bool taped = false;   // the forward wrote the whole window's tape
 };
 
 void adj_free(des_ctx *c)
@@ -317,7 +324,10 @@ int des_adjoint_forward(des_ctx *c, int nsteps, int checkpoint_every)
     w->recorded = false;
     if ((rc = alloc_buffers(c, w))) return rc;
     const size_t nn = c->nn, ne = c->ne;
-    const int nseg = (nsteps + checkpoint_every - 1) / checkpoint_every;
+    const bool taped = checkpoint_every >= nsteps;   // one segment: tape it now
+    const int C = taped ? nsteps : checkpoint_every;
+    const int nseg = (nsteps + C - 1) / C;
+    if (taped && (rc = alloc_tape(c, w, nsteps))) return rc;
     if ((int)w->ck.size() != nseg) {
         cudaFree(w->ck_mem);
         w->ck_mem = nullptr;
@@ -338,13 +348,15 @@ int des_adjoint_forward(des_ctx *c, int nsteps, int checkpoint_every)
     CKA(cudaStreamSynchronize(c->stream));
     w->dt = clk.dt;
     for (int k = 0; k < nsteps; ++k) {
-        if (k % checkpoint_every == 0) CKA(copy_state(w->ck[k / checkpoint_every], live_state(c), nn, ne, c->stream));
-        if ((rc = adj_step(c, nullptr))) return rc;
+        if (k % C == 0) CKA(copy_state(w->ck[k / C], live_state(c), nn, ne, c->stream));
+        if ((rc = adj_step(c, taped ? &w->tape[k] : nullptr))) return rc;
     }
+    if (taped) CKA(copy_state(tape_state(w->tape[nsteps]), live_state(c), nn, ne, c->stream));
     CKA(cudaMemcpyAsync(w->final_pool, c->pool, c->pool_bytes, cudaMemcpyDeviceToDevice, c->stream));
     w->K = nsteps;
-    w->C = checkpoint_every;
+    w->C = C;
     w->nseg = nseg;
+    w->taped = taped;
     w->recorded = true;
     return DES_OK;
 }
@@ -370,10 +382,12 @@ int des_adjoint_backward(des_ctx *c, const des_host_state *seed, des_host_state 
     }
     for (int seg = w->nseg - 1; seg >= 0; --seg) {
         const int k0 = seg * w->C, L = std::min(w->C, w->K - k0);
-        CKA(copy_state(live_state(c), w->ck[seg], nn, ne, s));
-        for (int j = 0; j < L; ++j)
-            if ((rc = adj_step(c, &w->tape[j]))) return rc;
-        CKA(copy_state(tape_state(w->tape[L]), live_state(c), nn, ne, s));
+        if (!w->taped) {   // recompute the segment from its checkpoint onto the tape
+            CKA(copy_state(live_state(c), w->ck[seg], nn, ne, s));
+            for (int j = 0; j < L; ++j)
+                if ((rc = adj_step(c, &w->tape[j]))) return rc;
+            CKA(copy_state(tape_state(w->tape[L]), live_state(c), nn, ne, s));
+        }
         for (int j = L - 1; j >= 0; --j)
             if ((rc = adj_reverse_step(c, w, w->tape[j], w->tape[j + 1]))) return rc;
     }

@@ -143,18 +143,25 @@ def test_reverse_log10_viscosity():
 
 def test_reverse_window_checkpointing_is_exact():
     """The gradients do not depend on the checkpoint spacing (the recompute
-    is bit-reproducible), and match the central difference over 12 steps."""
+    is bit-reproducible): 12 steps checkpointed every 5 equal the window
+    taped by its forward (checkpoint_every 12, and 100), also on a second
+    backward over the same tape; and they match the central difference."""
     rng = np.random.default_rng(4)
     win = _window(_workload(), 12, 5)
     seed = _seed(win, rng)
     win.run()
     s5, g5 = win.gradients(seed)
-    win.C = 12
-    win.run()
-    s12, g12 = win.gradients(seed)
-    for k in FIELDS:
-        np.testing.assert_array_equal(s5[k], s12[k], err_msg=k)
-    np.testing.assert_array_equal(g5["vbc_values"], g12["vbc_values"])
+    for C in (12, 100):
+        win.C = C
+        win.run()
+        for _ in range(2):
+            sC, gC = win.gradients(seed)
+            for k in FIELDS:
+                np.testing.assert_array_equal(s5[k], sC[k], err_msg=f"{k}, checkpoint_every {C}")
+            np.testing.assert_array_equal(g5["vbc_values"], gC["vbc_values"])
+            for k, g in g5.items():
+                if k != "vbc_values":
+                    np.testing.assert_array_equal(g, gC[k], err_msg=f"grad {k}, checkpoint_every {C}")
     win.C = 5
     for f in ("vel", "stress", "coord"):
         ad, fd, rel = _check(win, seed, dstate=_dstate(win, rng, f))
