@@ -447,6 +447,20 @@ def main():
     return 0
 
 
+def run_fitting_tape(win, params, spacings):
+    """win.run(params) with the first checkpoint spacing in `spacings` whose
+    tape (spacing + 1 step records) fits in device memory; leaves win.C at
+    that spacing."""
+    from dynearthsol_gb300 import capi
+    for i, C in enumerate(spacings):
+        win.C = C
+        try:
+            return win.run(params)
+        except capi.DesError as ex:
+            if ex.code != capi.DES_ENOMEM or i == len(spacings) - 1:
+                raise
+
+
 def adjoint_bench(args, stream):
     """Adjoint/forward wall-time ratio on the 998,400-tet adjoint case: a
     window of K FP64 steps (dt held) with a checkpoint every C steps (by
@@ -479,13 +493,9 @@ def adjoint_bench(args, stream):
     win = Window(m, init, clock0, K, C)
     nodes = top_nodes(wl.mesh)
     LV = capi.EF_LOG10_VISC
-    try:
-        target = win.run({LV: lv_t})["vel"]
-    except capi.DesError as ex:
-        if C < K or ex.code != capi.DES_ENOMEM:
-            raise
-        C = win.C = 50   # the window's tape does not fit: checkpoints every 50 steps
-        target = win.run({LV: lv_t})["vel"]
+    # the whole window as one segment when its tape fits, else every 50 steps
+    target = run_fitting_tape(win, {LV: lv_t}, [C] if C < K else [K, 50])["vel"]
+    C = win.C
 
     def loss_of(lv):
         return surface_velocity_misfit(win.run({LV: lv})["vel"], target, nodes)[0]
@@ -606,7 +616,8 @@ def heat_adjoint_bench(args, stream):
     interior nodes jittered by +-20% of the spacing, elements randomly
     permuted), EVP mechanics coupled with explicit heat (k = 3.3 W/m/K,
     cp = 1000 J/kg/K, radiogenic 1e-6 W/m^3).  1000 steps of the mixed step,
-    then an FP64 window of `heat_adjoint_steps` steps (checkpoint every 50)
+    then an FP64 window of `heat_adjoint_steps` steps (checkpoint spacing:
+    the largest of K, K/2 and 50 whose tape fits in device memory)
     whose loss is the final-temperature misfit against a target run with
     conductivity 3.3 (1 + 0.2 f), f a seeded Gaussian random field
     (correlation length 15 km); gradient with respect to the per-element
@@ -616,7 +627,7 @@ def heat_adjoint_bench(args, stream):
     from dynearthsol_gb300.adjoint import Window, fd5, grf_log10_visc
     from dynearthsol_gb300.config import initial_state, make_workload
     from dynearthsol_gb300.solver import DeviceModel
-    K, C = args.heat_adjoint_steps, 50
+    K = args.heat_adjoint_steps
     KC = capi.EF_THERM_COND
     t0 = time.perf_counter()
     wl = make_workload("c4_3d_heat_jitter")
@@ -638,8 +649,9 @@ def heat_adjoint_bench(args, stream):
     mid = mx.download()
     clock = mx.clock()
     mx.close()
-    win = Window(m, mid, clock, K, C)
-    T_target = win.run({KC: k_target})["temperature"]
+    win = Window(m, mid, clock, K, K)
+    T_target = run_fitting_tape(win, {KC: k_target}, [K, max(K // 2, 1), 50])["temperature"]
+    C = win.C
 
     def loss_of(k):
         T = win.run({KC: k})["temperature"]

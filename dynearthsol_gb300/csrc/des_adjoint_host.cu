@@ -7,11 +7,13 @@
 // (~367 B per tet each, the forward values the reverse kernels read).  At
 // 1M tets and 50 steps per segment that is ~18 GB of HBM.
 //
-// A window of one segment (checkpoint_every >= nsteps) is taped by the
-// forward itself: it writes each step's record as it goes, and the backward
-// runs the reverse kernels alone, with no recompute.  It needs the same
-// tape as the backward of a one-segment window would: 500 steps of the
-// 998,400-tet case are ~184 GB, which GB300's HBM holds.
+// The forward tapes the window's last segment itself: it writes each of
+// its steps' records as it goes, so the backward, which reverses that
+// segment first, recomputes only the others.  The tape is the one the
+// backward needs anyway.  A window of one segment (checkpoint_every >=
+// nsteps) is then taped whole, and its backward runs the reverse kernels
+// alone: 500 steps of the 998,400-tet case are ~184 GB, which GB300's HBM
+// holds.
 #include <algorithm>
 #include <vector>
 
@@ -107,7 +109,7 @@ struct AdjWork {
     int K = 0, C = 0, nseg = 0;
     double dt = 0;
     bool recorded = false;
-    bool taped = false;   // the forward wrote the whole window's tape
+    int tape_seg = -1;   // the segment whose records the tape holds (-1: none)
 };
 
 void adj_free(des_ctx *c)
@@ -171,8 +173,10 @@ int alloc_buffers(des_ctx *c, AdjWork *w)
     cv.add((void **)&e2f_off, (ne + 1) * sizeof(int));
     cv.add((void **)&e2f_ent, nbf * sizeof(int));
     cudaError_t e = cudaMalloc((void **)&w->buf_mem, cv.total());
-    if (e != cudaSuccess)
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();   // reported here, not at the next launch check
         return ctx_fail(c, DES_ENOMEM, "adjoint buffers: cudaMalloc(%zu bytes): %s", cv.total(), cudaGetErrorString(e));
+    }
     cv.assign(w->buf_mem);
     a.e2f_off = e2f_off;
     a.e2f_ent = e2f_ent;
@@ -188,44 +192,63 @@ int alloc_buffers(des_ctx *c, AdjWork *w)
     return DES_OK;
 }
 
+void add_tape_step(Carver &cv, TapeStep &t, size_t nn, size_t ne)
+{
+    const size_t D = sizeof(double);
+    cv.add((void **)&t.x, 3 * nn * D);
+    cv.add((void **)&t.v, 3 * nn * D);
+    cv.add((void **)&t.T, nn * D);
+    cv.add((void **)&t.s, 6 * ne * D);
+    cv.add((void **)&t.pls, ne * D);
+    cv.add((void **)&t.volo, ne * D);
+    cv.add((void **)&t.vol, ne * D);
+    cv.add((void **)&t.shp, 12 * ne * D);
+    cv.add((void **)&t.mass, nn * D);
+    cv.add((void **)&t.tmass, nn * D);
+    cv.add((void **)&t.voln, nn * D);
+    cv.add((void **)&t.edot, 6 * ne * D);
+    cv.add((void **)&t.tdot, nn * D);
+    cv.add((void **)&t.ntmp, nn * D);
+    cv.add((void **)&t.edv, ne * D);
+    cv.add((void **)&t.sstar, 6 * ne * D);
+    cv.add((void **)&t.dp, ne * D);
+    cv.add((void **)&t.rho, ne * D);
+    cv.add((void **)&t.dpn, nn * D);
+    cv.add((void **)&t.sss, 6 * ne * D);
+    cv.add((void **)&t.f, 3 * nn * D);
+    cv.add((void **)&t.visc, ne * D);
+    cv.add((void **)&t.evp, ne);
+}
+
 int alloc_tape(des_ctx *c, AdjWork *w, int cap)
 {
     if (w->tape_mem && w->cap == cap) return DES_OK;
     cudaFree(w->tape_mem);
     w->tape_mem = nullptr;
     w->cap = 0;
-    const size_t nn = c->nn, ne = c->ne, D = sizeof(double);
-    w->tape.assign(cap + 1, TapeStep{});
+    w->tape_seg = -1;
+    w->tape.clear();
+    const size_t nn = c->nn, ne = c->ne;
+    // the whole tape against the free device memory, before any allocation
+    // (the host records too are sized by cap)
+    TapeStep probe{};
+    Carver one;
+    add_tape_step(one, probe, nn, ne);
+    const size_t need = one.total() * ((size_t)cap + 1);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && need > free_b)
+        return ctx_fail(c, DES_ENOMEM, "adjoint tape of %d steps: %zu bytes, %zu free on the device", cap, need,
+                        free_b);
+    w->tape.assign((size_t)cap + 1, TapeStep{});
     Carver cv2;
-    for (auto &t : w->tape) {
-        cv2.add((void **)&t.x, 3 * nn * D);
-        cv2.add((void **)&t.v, 3 * nn * D);
-        cv2.add((void **)&t.T, nn * D);
-        cv2.add((void **)&t.s, 6 * ne * D);
-        cv2.add((void **)&t.pls, ne * D);
-        cv2.add((void **)&t.volo, ne * D);
-        cv2.add((void **)&t.vol, ne * D);
-        cv2.add((void **)&t.shp, 12 * ne * D);
-        cv2.add((void **)&t.mass, nn * D);
-        cv2.add((void **)&t.tmass, nn * D);
-        cv2.add((void **)&t.voln, nn * D);
-        cv2.add((void **)&t.edot, 6 * ne * D);
-        cv2.add((void **)&t.tdot, nn * D);
-        cv2.add((void **)&t.ntmp, nn * D);
-        cv2.add((void **)&t.edv, ne * D);
-        cv2.add((void **)&t.sstar, 6 * ne * D);
-        cv2.add((void **)&t.dp, ne * D);
-        cv2.add((void **)&t.rho, ne * D);
-        cv2.add((void **)&t.dpn, nn * D);
-        cv2.add((void **)&t.sss, 6 * ne * D);
-        cv2.add((void **)&t.f, 3 * nn * D);
-        cv2.add((void **)&t.visc, ne * D);
-        cv2.add((void **)&t.evp, ne);
-    }
+    for (auto &t : w->tape) add_tape_step(cv2, t, nn, ne);
     cudaError_t e = cudaMalloc((void **)&w->tape_mem, cv2.total());
-    if (e != cudaSuccess)
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();   // reported here, not at the next launch check
+        w->tape.clear();
         return ctx_fail(c, DES_ENOMEM, "adjoint tape of %d steps: cudaMalloc(%zu bytes): %s", cap, cv2.total(),
                         cudaGetErrorString(e));
+    }
     cv2.assign(w->tape_mem);
     w->cap = cap;
     return DES_OK;
@@ -324,10 +347,10 @@ int des_adjoint_forward(des_ctx *c, int nsteps, int checkpoint_every)
     w->recorded = false;
     if ((rc = alloc_buffers(c, w))) return rc;
     const size_t nn = c->nn, ne = c->ne;
-    const bool taped = checkpoint_every >= nsteps;   // one segment: tape it now
-    const int C = taped ? nsteps : checkpoint_every;
-    const int nseg = (nsteps + C - 1) / C;
-    if (taped && (rc = alloc_tape(c, w, nsteps))) return rc;
+    const int C = std::min(checkpoint_every, nsteps);
+    const int nseg = (nsteps + C - 1) / C, last0 = (nseg - 1) * C;
+    w->tape_seg = -1;
+    if ((rc = alloc_tape(c, w, C))) return rc;
     if ((int)w->ck.size() != nseg) {
         cudaFree(w->ck_mem);
         w->ck_mem = nullptr;
@@ -337,6 +360,7 @@ int des_adjoint_forward(des_ctx *c, int nsteps, int checkpoint_every)
         cudaError_t e = cudaMalloc((void **)&w->ck_mem, cv.total());
         if (e != cudaSuccess) {
             w->ck.clear();
+            (void)cudaGetLastError();   // reported here, not at the next launch check
             return ctx_fail(c, DES_ENOMEM, "adjoint checkpoints: cudaMalloc(%zu bytes): %s", cv.total(),
                             cudaGetErrorString(e));
         }
@@ -349,14 +373,14 @@ int des_adjoint_forward(des_ctx *c, int nsteps, int checkpoint_every)
     w->dt = clk.dt;
     for (int k = 0; k < nsteps; ++k) {
         if (k % C == 0) CKA(copy_state(w->ck[k / C], live_state(c), nn, ne, c->stream));
-        if ((rc = adj_step(c, taped ? &w->tape[k] : nullptr))) return rc;
+        if ((rc = adj_step(c, k >= last0 ? &w->tape[k - last0] : nullptr))) return rc;
     }
-    if (taped) CKA(copy_state(tape_state(w->tape[nsteps]), live_state(c), nn, ne, c->stream));
+    CKA(copy_state(tape_state(w->tape[nsteps - last0]), live_state(c), nn, ne, c->stream));
     CKA(cudaMemcpyAsync(w->final_pool, c->pool, c->pool_bytes, cudaMemcpyDeviceToDevice, c->stream));
     w->K = nsteps;
     w->C = C;
     w->nseg = nseg;
-    w->taped = taped;
+    w->tape_seg = nseg - 1;
     w->recorded = true;
     return DES_OK;
 }
@@ -382,11 +406,13 @@ int des_adjoint_backward(des_ctx *c, const des_host_state *seed, des_host_state 
     }
     for (int seg = w->nseg - 1; seg >= 0; --seg) {
         const int k0 = seg * w->C, L = std::min(w->C, w->K - k0);
-        if (!w->taped) {   // recompute the segment from its checkpoint onto the tape
+        if (w->tape_seg != seg) {   // recompute the segment from its checkpoint onto the tape
+            w->tape_seg = -1;
             CKA(copy_state(live_state(c), w->ck[seg], nn, ne, s));
             for (int j = 0; j < L; ++j)
                 if ((rc = adj_step(c, &w->tape[j]))) return rc;
             CKA(copy_state(tape_state(w->tape[L]), live_state(c), nn, ne, s));
+            w->tape_seg = seg;
         }
         for (int j = L - 1; j >= 0; --j)
             if ((rc = adj_reverse_step(c, w, w->tape[j], w->tape[j + 1]))) return rc;

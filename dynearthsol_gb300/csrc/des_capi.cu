@@ -39,6 +39,10 @@ namespace {
 
 int cuda_fail(des_ctx *c, cudaError_t e, const char *what)
 {
+    // a failed call (an allocation, say) leaves its error as the runtime's
+    // last error, which the next launch check would report as its own;
+    // sticky errors stay whatever this returns
+    (void)cudaGetLastError();
     std::string &dst = c ? c->err : g_create_error;
     return fail_msg(dst, DES_ECUDA, "%s: %s", what, cudaGetErrorString(e));
 }
@@ -401,6 +405,7 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     for (auto &s : slots) total += s.bytes;
     cudaError_t ce = cudaMalloc((void **)&c->pool, total);
     if (ce != cudaSuccess) {
+        (void)cudaGetLastError();   // the failed allocation is reported here, not at the next launch
         int code = fail_msg(g_create_error, DES_ENOMEM, "cudaMalloc(%zu bytes): %s", total, cudaGetErrorString(ce));
         if (c->own_stream) cudaStreamDestroy(c->stream);
         delete c;

@@ -143,15 +143,18 @@ def test_reverse_log10_viscosity():
 
 def test_reverse_window_checkpointing_is_exact():
     """The gradients do not depend on the checkpoint spacing (the recompute
-    is bit-reproducible): 12 steps checkpointed every 5 equal the window
-    taped by its forward (checkpoint_every 12, and 100), also on a second
-    backward over the same tape; and they match the central difference."""
+    is bit-reproducible): 12 steps checkpointed every 5 (the forward tapes
+    the last segment, the backward recomputes the other two) equal 12 steps
+    checkpointed every 3 and the window taped whole by its forward
+    (checkpoint_every 12, and 100).  A second backward, which finds the
+    tape holding the first segment, gives the same bits.  The gradients
+    match the central difference."""
     rng = np.random.default_rng(4)
     win = _window(_workload(), 12, 5)
     seed = _seed(win, rng)
     win.run()
     s5, g5 = win.gradients(seed)
-    for C in (12, 100):
+    for C in (5, 3, 12, 100):
         win.C = C
         win.run()
         for _ in range(2):
@@ -312,3 +315,27 @@ def test_reverse_torch_autograd_function():
     rel = abs(fd - ad) / max(abs(fd), abs(ad))
     print(f"  autograd: adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
     assert rel <= 1e-5, rel
+
+
+def test_window_tape_too_large_is_enomem_and_context_survives():
+    """A window whose tape cannot fit on the device (1000 steps of the
+    998,400-tet case, ~367 GB) is refused with DES_ENOMEM before any
+    allocation, and the context keeps working: the next upload and step run
+    and leave no device error."""
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import initial_state, make_workload
+    from dynearthsol_gb300.solver import DeviceModel
+    wl = make_workload("c1_3d_evp")
+    st, cp = initial_state(wl)
+    m = DeviceModel(wl, comp_pressure=cp)
+    init = m.init_fields(st)
+    clk = m.clock()
+    with pytest.raises(capi.DesError) as ex:
+        m.adjoint_forward(1000, 1000)
+    assert ex.value.code == capi.DES_ENOMEM, ex.value
+    m.upload(init, clk)
+    m.step(2)
+    m.sync()
+    assert m.device_status() == 0
+    assert np.isfinite(m.download()["vel"]).all()
+    m.close()
