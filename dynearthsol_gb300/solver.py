@@ -171,7 +171,9 @@ class DeviceModel:
     ADJOINT_FIELDS = ("coord", "vel", "temperature", "stress", "plstrain")
 
     def adjoint_forward(self, nsteps: int, checkpoint_every: int):
-        """Run a window of nsteps steps (dt held) recording checkpoints."""
+        """Run a window of nsteps steps (dt held) recording a checkpoint every
+        checkpoint_every steps and the last segment's tape (the whole
+        window's when checkpoint_every >= nsteps)."""
         self._check(self.lib.des_adjoint_forward(self.ctx, nsteps, checkpoint_every))
 
     def adjoint_backward(self, seed: dict, want_start: bool = True):
