@@ -33,6 +33,23 @@ __device__ __forceinline__ double tshp(const TapeStep &t, size_t ne, int k, int 
     return t.shp[((size_t)k * 4 + i) * ne + e];
 }
 
+// the stress after NMD_stress (geometry.cxx:182-236), as k_nmd_correct forms
+// it, from the tape's stress after update_stress and its pressure changes:
+// the same operations in the same order, so the same bits (the division by
+// 4 is exact, with or without a fused multiply-add)
+__device__ __forceinline__ void tape_sss(const KP &p, const TapeStep &t, int e, double *s)
+{
+    const size_t ne = p.ne;
+    double dpn = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dpn += t.dpn[conn_at(p, i, e)];
+    const double corr = divnd<3>(-t.dp[e] + dpn / 4);
+#pragma unroll
+    for (int cc = 0; cc < 6; ++cc) s[cc] = t.sstar[cc * ne + e];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) s[i] += corr;
+}
+
 __device__ __forceinline__ void tload3(const double *a, size_t nn, int n, double *o)
 {
     o[0] = a[n];
@@ -163,11 +180,9 @@ __global__ void __launch_bounds__(TPB_A) k_adj_end_geometry(KP p, AdjBufs a, Tap
     double gv[4][3] = {};
     if (p.mat.rheol_type & DES_RH_ELASTIC) {
         double s[6], g[6];
+        tape_sss(p, t, e, s);
 #pragma unroll
-        for (int cc = 0; cc < 6; ++cc) {
-            s[cc] = t.sss[cc * ne + e];
-            g[cc] = a.as[cc * ne + e];
-        }
+        for (int cc = 0; cc < 6; ++cc) g[cc] = a.as[cc * ne + e];
         double sh[3][4];
 #pragma unroll
         for (int k = 0; k < 3; ++k)
@@ -440,11 +455,9 @@ __global__ void __launch_bounds__(TPB_A) k_adj_force(KP p, AdjBufs a, TapeStep t
     if (e >= p.ne) return;
     const size_t ne = p.ne, nn = p.nn;
     double s[6], gsig[6];
+    tape_sss(p, t, e, s);
 #pragma unroll
-    for (int cc = 0; cc < 6; ++cc) {
-        s[cc] = t.sss[cc * ne + e];
-        gsig[cc] = a.as[cc * ne + e];
-    }
+    for (int cc = 0; cc < 6; ++cc) gsig[cc] = a.as[cc * ne + e];
     const double vol = t.vol[e];
     const double gravity = p.prm.gravity;
     const double buoy = (gravity != 0) ? t.rho[e] * gravity / 4 : 0.0;

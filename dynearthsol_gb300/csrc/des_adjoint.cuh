@@ -30,7 +30,6 @@ struct TapeStep {
     double *dp;      // [ne] dpressure
     double *rho;     // [ne] element density of the step
     double *dpn;     // [nn] NMD nodal pressure change
-    double *sss;     // [6][ne] stress after NMD_stress (before the rotation)
     double *f;       // [3][nn] force after damping
     double *visc;    // [ne] viscosity the rheology used (Maxwell, EVP)
     unsigned char *evp;   // [ne] EVP branch taken: 1 elasto-plastic, 0 Maxwell

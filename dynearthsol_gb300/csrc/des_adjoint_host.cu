@@ -4,15 +4,16 @@
 //
 // Memory: a checkpoint holds the state and its derived fields (~180 B per
 // tet); the tape of one segment holds checkpoint_every + 1 step records
-// (~367 B per tet each, the forward values the reverse kernels read).  At
-// 1M tets and 50 steps per segment that is ~18 GB of HBM.
+// (~319 B per tet each, the forward values the reverse kernels read; the
+// stress after NMD_stress is rebuilt from them).  At 1M tets and 50 steps
+// per segment that is ~16 GB of HBM.
 //
 // The forward tapes the window's last segment itself: it writes each of
 // its steps' records as it goes, so the backward, which reverses that
 // segment first, recomputes only the others.  The tape is the one the
 // backward needs anyway.  A window of one segment (checkpoint_every >=
 // nsteps) is then taped whole, and its backward runs the reverse kernels
-// alone: 500 steps of the 998,400-tet case are ~184 GB, which GB300's HBM
+// alone: 500 steps of the 998,400-tet case are ~160 GB, which GB300's HBM
 // holds.
 #include <algorithm>
 #include <vector>
@@ -214,7 +215,6 @@ void add_tape_step(Carver &cv, TapeStep &t, size_t nn, size_t ne)
     cv.add((void **)&t.dp, ne * D);
     cv.add((void **)&t.rho, ne * D);
     cv.add((void **)&t.dpn, nn * D);
-    cv.add((void **)&t.sss, 6 * ne * D);
     cv.add((void **)&t.f, 3 * nn * D);
     cv.add((void **)&t.visc, ne * D);
     cv.add((void **)&t.evp, ne);
@@ -290,7 +290,6 @@ int adj_step(des_ctx *c, const TapeStep *t)
     n += launch_nmd_gather(p, s);
     if (t) CKA(cp(t->dpn, p.ntmp, nn));
     n += launch_nmd_correct(p, s, true);
-    if (t) CKA(cp(t->sss, p.stress, 6 * ne));
     n += launch_force(p, s, true);
     if (t) CKA(cp(t->f, p.f, 3 * nn));
     // mass from the geometry pass's element terms: the same sums, in the same
