@@ -465,7 +465,7 @@ def adjoint_bench(args, stream):
     """Adjoint/forward wall-time ratio on the 998,400-tet adjoint case: a
     window of K FP64 steps (dt held) with a checkpoint every C steps (by
     default the whole window as one segment, whose tape the forward records,
-    ~184 GB for 500 steps; checkpoints every 50 steps when device memory is
+    ~160 GB for 500 steps; checkpoints every 50 steps when device memory is
     short); loss =
     the top-surface velocity misfit against a target run whose log10
     viscosity field is a seeded Gaussian random field (mean 21, sd 0.5,

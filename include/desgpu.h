@@ -335,7 +335,7 @@ int des_write_save(des_ctx *ctx, const char *filename);
  * des_adjoint_forward runs the window from the current state, keeping the
  * state every checkpoint_every steps, and leaves the context at the
  * window's end.  It also records the tape of the window's last segment
- * (checkpoint_every + 1 step records of ~367 bytes per tet, the tape the
+ * (checkpoint_every + 1 step records of ~319 bytes per tet, the tape the
  * backward needs anyway).  des_adjoint_backward takes the adjoint of that
  * final state in seed (its fields coord, vel, temperature, stress and
  * plstrain, in des_host_state's layout; NULL fields are zero), recomputes
