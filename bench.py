@@ -697,11 +697,13 @@ def run_e2e(args, m, wl, init, clock0, world, dist):
         pinned[k] = (tt, a)
     hs = {k: a for k, (tt, a) in pinned.items()}
     # bytes des_step_host moves per call: every array of the state, less the
-    # fields the step overwrites before reading them (not uploaded) and those
-    # no step writes (not downloaded)
+    # fields the step overwrites before reading them and, on the slab-pipelined
+    # path (one step per call), the geometric fields it forms from the uploaded
+    # coordinates (not uploaded), and those no step writes (not downloaded)
     total = {k: a.nbytes for k, a in hs.items() if k != "shpdy" or wl.mesh.ndims == 3}
+    formed = ("volume", "shpdx", "shpdy", "shpdz", "volume_n") + (("mass",) if wl.params.is_quasi_static else ())
     h2d = sum(v for k, v in total.items()
-              if k not in ("strain_rate", "force", "dpressure", "edvoldt", "ntmp"))
+              if k not in ("strain_rate", "force", "dpressure", "edvoldt", "ntmp") + formed)
     unwritten = ("coord0",) if wl.mat.is_plane_strain else ("coord0", "stressyy")
     d2h = sum(v for k, v in total.items() if k not in unwritten)
     clk = clock0

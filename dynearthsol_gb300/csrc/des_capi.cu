@@ -540,6 +540,7 @@ int des_destroy(des_ctx *c)
         cudaStreamSynchronize(c->ystream);
         cudaStreamDestroy(c->ystream);
         for (cudaEvent_t e : c->pipe_ev) cudaEventDestroy(e);
+        cudaFree(c->d_pipe_sink);
     }
     if (c->xstream) {
         cudaStreamSynchronize(c->xstream);
@@ -1188,8 +1189,14 @@ struct SlabField {
 };
 
 // The fields of one call, or false when the call does not qualify: the
-// state must be complete (the derived fields and coord0 given, as the
+// state must be complete (coord0 and the derived fields given, as the
 // reference's Variables hold them) and page-locked (graph copy nodes).
+// Volume, shape functions and volume_n are functions of the coordinates,
+// and in the quasi-static mode so is the mass (pseudo-density x volume /
+// NPE): the step forms them on the device from the uploaded coordinates,
+// with the kernels and bits of its own update_mesh, instead of uploading
+// them (~108 MB of the 998,400-tet state).  tmass is uploaded: the
+// reference's init forms it before it sets the temperature.
 bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &out)
 {
     KP &p = c->kp;
@@ -1197,6 +1204,7 @@ bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &o
     const size_t shp1 = (size_t)ne * npe;
     float *s32 = use_mixed(c) ? p.shp32 : nullptr;
     const bool ps = p.mat.is_plane_strain != 0;
+    const bool qs = p.prm.is_quasi_static != 0;
     // up: needed by the step; down: written by it (strain_rate, force,
     // dpressure, edvoldt and ntmp are written before they are read; coord0
     // and, outside plane strain, stressyy are never written)
@@ -1206,11 +1214,11 @@ bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &o
         {st->vel, p.v, nullptr, nd, true, true, true, nullptr},
         {st->force, p.f, nullptr, nd, true, false, true, nullptr},
         {st->temperature, p.T, nullptr, 1, true, true, true, nullptr},
-        {st->mass, p.mass, nullptr, 1, true, true, true, nullptr},
+        {st->mass, p.mass, nullptr, 1, true, !qs, true, nullptr},
         {st->tmass, p.tmass, nullptr, 1, true, true, true, nullptr},
-        {st->volume_n, p.vol_n, nullptr, 1, true, true, true, nullptr},
+        {st->volume_n, p.vol_n, nullptr, 1, true, false, true, nullptr},
         {st->ntmp, p.ntmp, nullptr, 1, true, false, true, nullptr},
-        {st->volume, p.vol, nullptr, 1, false, true, true, nullptr},
+        {st->volume, p.vol, nullptr, 1, false, false, true, nullptr},
         {st->volume_old, p.vol_old, nullptr, 1, false, true, true, nullptr},
         {st->stress, p.stress, nullptr, nstr, false, true, true, nullptr},
         {st->strain, p.strain, nullptr, nstr, false, true, true, nullptr},
@@ -1220,9 +1228,9 @@ bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &o
         {st->stressyy, p.syy, nullptr, 1, false, true, ps, nullptr},
         {st->dpressure, p.dp, nullptr, 1, false, false, true, nullptr},
         {st->edvoldt, p.edvoldt, nullptr, 1, false, false, true, nullptr},
-        {st->shpdx, p.shp, s32, npe, false, true, true, nullptr},
-        {nd == 3 ? st->shpdy : nullptr, p.shp + shp1, s32 ? s32 + shp1 : nullptr, npe, false, nd == 3, nd == 3, nullptr},
-        {st->shpdz, p.shp + (size_t)(nd - 1) * shp1, s32 ? s32 + (size_t)(nd - 1) * shp1 : nullptr, npe, false, true, true,
+        {st->shpdx, p.shp, s32, npe, false, false, true, nullptr},
+        {nd == 3 ? st->shpdy : nullptr, p.shp + shp1, s32 ? s32 + shp1 : nullptr, npe, false, false, nd == 3, nullptr},
+        {st->shpdz, p.shp + (size_t)(nd - 1) * shp1, s32 ? s32 + (size_t)(nd - 1) * shp1 : nullptr, npe, false, false, true,
          nullptr},
     };
     out.clear();
@@ -1265,7 +1273,12 @@ bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &o
 // uploads (xstream), coarse slab b uploads the element fine slabs [C_b,
 // C_b+1) and the node fine slabs [C_b + 1, C_b+1 + 1), all that slab b's first
 // stage reads; downloads (ystream), once slab b has run, the fine slabs
-// [C_b - 3, C_b+1 - 3), which no later stage writes.
+// [C_b - 4, C_b+1 - 4), which no later stage writes.  Two stages lead the
+// step's eight: an element pass that forms the volume, shape functions and
+// mass terms from the uploaded coordinates (those fields are not uploaded)
+// and a node pass that sums mass and volume_n, so the skew is
+// 0,0,1,1,2,2,3,3,4,4.  The uploaded tmass (and, outside the quasi-static
+// mode, mass) is kept: the node pass writes those sums to a scratch sink.
 int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec_t *exec, int *nkern)
 {
     const int B = c->nslab, NF = c->nfine;
@@ -1274,7 +1287,8 @@ int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec
     const bool thermal = p0.prm.has_thermal_diffusion != 0;
     cudaStream_t cs = c->stream, xs = c->xstream, ys = c->ystream;
     std::vector<cudaEvent_t> &ev = c->pipe_ev;   // [0,B) uploaded, [B,2B) slab done, 2B fork, 2B+1/2 joins
-    static const int SKEW[8] = {0, 0, 1, 1, 2, 2, 3, 3};
+    constexpr int NSTAGE = 10, LAG = 4;
+    static const int SKEW[NSTAGE] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 4};
     auto cb = [&](int b) { return (int)((long long)NF * b / B); };   // C_b
     // a fine-slab range, clipped to [0, NF); the last coarse slab runs to NF
     auto fine = [&](int b, int shift, int &lo, int &hi) {
@@ -1316,7 +1330,7 @@ int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec
     // the step, coarse slab by coarse slab
     for (int b = 0; b < B; ++b) {
         CKC(cudaStreamWaitEvent(cs, ev[b], 0));
-        for (int st = 0; st < 8; ++st) {
+        for (int st = 0; st < NSTAGE; ++st) {
             int lo, hi;
             fine(b, SKEW[st], lo, hi);
             if (hi <= lo) continue;
@@ -1326,19 +1340,32 @@ int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec
             q.f_lo = c->slab_f[lo], q.f_hi = c->slab_f[hi];
             q.fac_order = c->d_fac_order;
             switch (st) {
-            case 0: n += mixed ? launch_elem_pass_mixed(q, cs, thermal) : launch_elem_pass(q, cs, thermal); break;
-            case 1: n += mixed ? launch_node_pass_mixed(q, cs, thermal) : launch_node_pass(q, cs, thermal); break;
-            case 2: n += mixed ? launch_update_stress_mixed(q, cs, true) : launch_update_stress(q, cs, true); break;
-            case 3: n += launch_nmd_gather(q, cs); break;
-            case 4: n += launch_nmd_correct(q, cs, true); break;
-            case 5: n += launch_force(q, cs, true, mixed); break;
-            case 6: {
+            case 0: {   // the derived fields of the start state: the element density from T, as compute_mass forms it
+                KP g = q;
+                g.rho_e = nullptr;
+                n += launch_geometry(g, cs, GEO_VOLUME | GEO_SHAPE | GEO_MASS_TERMS);
+                break;
+            }
+            case 1: {   // mass (quasi-static) and volume_n; the uploaded tmass (and mass) stay
+                KP g = q;
+                g.tmass = c->d_pipe_sink;
+                if (!g.prm.is_quasi_static) g.mass = c->d_pipe_sink + c->nn;
+                n += launch_mass_sum(g, cs);
+                break;
+            }
+            case 2: n += mixed ? launch_elem_pass_mixed(q, cs, thermal) : launch_elem_pass(q, cs, thermal); break;
+            case 3: n += mixed ? launch_node_pass_mixed(q, cs, thermal) : launch_node_pass(q, cs, thermal); break;
+            case 4: n += mixed ? launch_update_stress_mixed(q, cs, true) : launch_update_stress(q, cs, true); break;
+            case 5: n += launch_nmd_gather(q, cs); break;
+            case 6: n += launch_nmd_correct(q, cs, true); break;
+            case 7: n += launch_force(q, cs, true, mixed); break;
+            case 8: {
                 int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP | GEO_MASS_TERMS;
                 if (q.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;
                 n += launch_geometry(q, cs, geo);
                 break;
             }
-            case 7: n += launch_mass_sum(q, cs); break;
+            case 9: n += launch_mass_sum(q, cs); break;
             }
             CKC(cudaGetLastError());
         }
@@ -1350,7 +1377,7 @@ int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec
     for (int b = 0; b < B; ++b) {
         CKC(cudaStreamWaitEvent(ys, ev[B + b], 0));
         int flo, fhi;
-        fine(b, 3, flo, fhi);
+        fine(b, LAG, flo, fhi);
         RowTable t{};
         for (const SlabField &f : F) {
             if (!f.down || f.ncomp == 1) continue;
@@ -1394,6 +1421,7 @@ int ensure_pipe(des_ctx *c)
     if (c->ystream) return DES_OK;
     c->pipe_ev.assign(2 * c->nslab + 3, nullptr);
     for (cudaEvent_t &e : c->pipe_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CK(cudaMalloc((void **)&c->d_pipe_sink, 2 * (size_t)c->nn * sizeof(double)));
     CK(cudaStreamCreateWithFlags(&c->ystream, cudaStreamNonBlocking));
     return DES_OK;
 }

@@ -51,6 +51,7 @@ struct des_ctx {
     cudaGraphExec_t pipe_exec = nullptr;   // the pipelined host step, for the host arrays below
     std::vector<const void *> pipe_key;
     std::vector<cudaEvent_t> pipe_ev;
+    double *d_pipe_sink = nullptr;         // [2][nn]: node sums the pipelined step forms but keeps uploaded
     int pipe_kernels = 0;
     int step_kernels = 0;
     long long launches = 0;
