@@ -282,7 +282,11 @@ int des_step(des_ctx *ctx, int nsteps);
  * a complete page-locked state and a mesh numbered slab by slab (as the
  * structured box meshes are), the upload, the step and the download overlap
  * slab by slab (one CUDA graph, built on the first such call for these host
- * arrays and reused while they stay the same). */
+ * arrays and reused while they stay the same).  That call also forms volume,
+ * the shape functions, volume_n and, quasi-static, mass from the uploaded
+ * coordinates with the kernels of the step's own update_mesh, instead of
+ * uploading them (as the reference's loop keeps them: functions of the
+ * coordinates); it still downloads them.  tmass is uploaded. */
 int des_step_host(des_ctx *ctx, des_host_state *st, int nsteps);
 
 /* ---- output frames in the reference's .save format ---------------------
