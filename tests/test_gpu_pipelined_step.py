@@ -122,3 +122,16 @@ def test_pipelined_2d():
     wl = make_workload("c0_2d_ep", cells=(32, 4))
     per_call = _run(wl, capi.PREC_FP64, 12)
     assert _pipelined(per_call, 4), per_call
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_pipelined_dynamic_mode(prec):
+    """Not quasi-static, without heat diffusion: the mass is the density's
+    (uploaded, like tmass, not formed on the device), 16 x 4 x 3 cubes."""
+    from dataclasses import replace
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import make_workload
+    wl = make_workload("c1_3d_evp", cells=(16, 4, 3))
+    wl.params = replace(wl.params, is_quasi_static=False, has_thermal_diffusion=False)
+    per_call = _run(wl, capi.PREC_FP64 if prec == "fp64" else capi.PREC_MIXED, 12)
+    assert _pipelined(per_call, 4), per_call
