@@ -172,3 +172,57 @@ def test_pairs_reach_the_pressure_term():
     with np.errstate(invalid="ignore"):
         exact = (second_invariant2(a) < second_invariant2(b)).astype(int)
     assert ((dec >= 0) & (dec != exact)).sum() > 100
+
+
+# ---- the mixed EVP branch's trial deviator --------------------------------
+# k_update_stress_mixed3 runs both screens on qt = x + y, x_i = s_i - s0 (the
+# old normal deviator, s0 = div3 of the old trace) and y_i = 2G (de_i -
+# div3(tr de)), instead of the deviator of the FP64 trial stress that
+# elastic_mixed forms (s_i + fma(2G, de_i, lambda tr de)), whose mean and
+# deviator second_invariant2_ then takes.  Its comment bounds the distance
+# by 22 u S, S = |s0| + sum |x_i| + sum |y_i| + (2G + 2K) sum |de_i|.
+
+def _fma_vec(a, b, c):
+    import ctypes
+    import ctypes.util
+    libm = ctypes.CDLL(ctypes.util.find_library("m"))
+    libm.fma.restype = ctypes.c_double
+    libm.fma.argtypes = (ctypes.c_double,) * 3
+    return np.array([libm.fma(float(p), float(q), float(r)) for p, q, r in zip(a, b, c)])
+
+
+def test_trial_deviator_from_shared_terms_is_within_22uS():
+    rng = np.random.default_rng(21)
+    n = 20_000
+    u = 2.0 ** -53
+    K = 10 ** rng.uniform(9, 11.5, n)
+    G = K * rng.uniform(0.1, 1.5, n)   # Poisson's ratio from about 0.43 down to below zero
+    P = np.where(rng.random(n) < 0.9, -1, 1) * 10 ** rng.uniform(0, 10, n)
+    dev = rng.standard_normal((n, 3))
+    dev -= dev.mean(axis=1, keepdims=True)
+    s_old = P[:, None] + dev * (np.abs(P) * 10 ** rng.uniform(-12, 0, n))[:, None]
+    # increments whose deviatoric part nearly cancels the old deviator (y ~ -x)
+    # in a third of the cases, with a volumetric part up to the pressure's size
+    c = np.where(rng.random(n) < 0.33, 1 + 10 ** rng.uniform(-12, -1, n), rng.uniform(-3, 3, n))
+    de = -c[:, None] * (s_old - s_old.mean(axis=1, keepdims=True)) / (2 * G[:, None])
+    de += (10 ** rng.uniform(-12, -2, n) * np.abs(P) / K * rng.standard_normal(n))[:, None]
+    de *= 1 + 1e-3 * rng.standard_normal((n, 3))
+    # the kernel's terms
+    trde = (de[:, 0] + de[:, 1]) + de[:, 2]
+    s0 = ((s_old[:, 0] + s_old[:, 1]) + s_old[:, 2]) / 3
+    dv3 = trde / 3
+    g2 = 2 * G
+    x = s_old - s0[:, None]
+    y = g2[:, None] * (de - dv3[:, None])
+    qt = x + y
+    S = np.abs(s0) + np.abs(x).sum(axis=1) + np.abs(y).sum(axis=1) + (2 * g2 + 2 * K) * np.abs(de).sum(axis=1)
+    # the FP64 trial stress and the deviator second_invariant2_ forms from it
+    lam = K - 2. / 3 * G
+    ldev = lam * trde
+    sp = np.stack([s_old[:, i] + _fma_vec(g2, de[:, i], ldev) for i in range(3)], axis=1)
+    am = ((sp[:, 0] + sp[:, 1]) + sp[:, 2]) / 3
+    q = sp - am[:, None]
+    dist = np.abs(qt - q).max(axis=1)
+    assert (dist <= 22 * u * S).all(), (dist / (u * S)).max()
+    # and the bound is not loose by more than a few orders of magnitude
+    assert (dist / (u * S)).max() > 0.05
