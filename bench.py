@@ -221,6 +221,23 @@ def config_of(args, wl):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+def max_over_ranks(value: float, dist, device: str = "cuda") -> float:
+    """The largest of every rank's value (the job's time is its slowest
+    rank's); the value itself without a process group."""
+    if not dist:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_value(units_per_rank: float, seconds: float, world: int) -> float:
+    """Whole-job throughput in millions of units per second: the units all
+    ranks processed over the slowest rank's time."""
+    return world * units_per_rank / seconds / 1e6
+
+
 def timed_steps(m, stream, steps, warmup, dist, sample_clocks=False, local=0):
     """W untimed steps, then K steps between CUDA events on the library's
     stream (barrier + synchronize on both sides); returns (ms, launches,
@@ -245,11 +262,7 @@ def timed_steps(m, stream, steps, warmup, dist, sample_clocks=False, local=0):
     status = m.device_status()
     if status:
         raise RuntimeError(f"device status {status:#x} during the timed run")
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    return ms, m.launches() - l0, clocks
+    return max_over_ranks(ms, dist), m.launches() - l0, clocks
 
 
 def error_gate(wl, init, clock0, cp, stream, nsteps):
@@ -350,7 +363,7 @@ def main():
 
     # ---- headline: device-resident throughput of the selected precision ----
     ms, launches, clocks = timed_steps(m, stream, args.steps, args.warmup, dist, True, local)
-    value = world * ne * args.steps / (ms / 1e3) / 1e6
+    value = aggregate_value(ne * args.steps, ms / 1e3, world)
     compare = None
     if args.precision == "mixed" and not args.no_compare:
         ms64, _, _ = timed_steps(f64, stream, args.steps, args.warmup, dist)
@@ -358,7 +371,7 @@ def main():
         l2 = float(np.linalg.norm(b["stress"] - a["stress"]) / np.linalg.norm(a["stress"]))
         maxn = {k: float(np.abs(b[k] - a[k]).max() / max(np.abs(a[k]).max(), 1e-300))
                 for k in ("vel", "stress", "strain", "temperature", "plstrain", "coord", "force")}
-        compare = {"fp64_value": world * ne * args.steps / (ms64 / 1e3) / 1e6, "fp64_ms_per_step": ms64 / args.steps,
+        compare = {"fp64_value": aggregate_value(ne * args.steps, ms64 / 1e3, world), "fp64_ms_per_step": ms64 / args.steps,
                    "speedup_mixed_over_fp64": ms64 / ms,
                    "stress_rel_l2_err_vs_fp64": l2, "gate": 1e-6,
                    "steps_compared": args.warmup + args.steps,
@@ -718,10 +731,7 @@ def run_e2e(args, m, wl, init, clock0, world, dist):
         clk = m.step_host(hs, 1, clk)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * ne * args.e2e_steps / float(te.item()) / 1e6
+    e2e_value = aggregate_value(ne * args.e2e_steps, max_over_ranks(e2e_s, dist), world)
     return {"value": e2e_value, "unit": "Mtet-steps/s", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
             "call": "des_step_host (pinned host state, reference AoS layout, 1 step per call)"}
