@@ -105,3 +105,23 @@ def test_other_laws():
             if mat["vmin"] < v64 < mat["vmax"]:
                 worst = max(worst, abs(visc_mixed(mat, e, T) - v64) / v64)
         assert worst < 3e-7, (mat["n"], worst)
+
+
+def test_maxwell_coefficients_in_fp32():
+    """maxwell_coef (csrc/des_mixed.cu): tmp = dt G / (2 visc) and
+    f2 - 1 = -tmp / (1 + tmp) formed in FP32, each within ~2^-22 of itself
+    (2^-21 asserted), over the time steps, moduli and viscosities of the
+    workloads and beyond."""
+    rng = np.random.default_rng(9)
+    worst_t = worst_u = 0.0
+    for _ in range(20_000):
+        dt = 10 ** rng.uniform(3, 9)
+        G = 10 ** rng.uniform(9, 11.5)
+        visc = 10 ** rng.uniform(17, 25)
+        tf = (F(0.5) * F(dt) * F(G)) / F(visc)
+        uf = -tf / (F(1) + tf)
+        tmp = 0.5 * dt * G / visc
+        u = -tmp / (1 + tmp)
+        worst_t = max(worst_t, abs(float(tf) - tmp) / tmp)
+        worst_u = max(worst_u, abs(float(uf) - u) / abs(u))
+    assert worst_t < 2.0 ** -21 and worst_u < 2.0 ** -21, (worst_t, worst_u)
