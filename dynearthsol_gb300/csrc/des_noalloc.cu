@@ -13,6 +13,7 @@
 // scratch the smoothing needs -- the per-node pressure sum -- lives in the
 // fixed array below, which every GPU that loads this library holds until the
 // process exits.
+#include <atomic>
 #include <cstdio>
 #include <cuda_runtime.h>
 
@@ -23,10 +24,17 @@ namespace {
 // per-node scratch: DES_NOALLOC_MAX_NODES doubles (16 MiB per device)
 __device__ __align__(256) double g_nmd_scratch[DES_NOALLOC_MAX_NODES];
 
+// Device address of the scratch, per device.  In host code g_nmd_scratch
+// names a host-side stand-in, so the kernels get this address instead.  It
+// is looked up again on every call made outside stream capture (a device
+// reset reloads the module and can move the array); inside a capture, where
+// the lookup is not allowed, the address of the last lookup on this device
+// is used.  Relaxed atomics: concurrent first calls all store the same
+// value, and nothing else is ordered by it.
 constexpr int kMaxDevices = 64;
-double *g_scratch_addr[kMaxDevices] = {};   // device address of the scratch, per device
+std::atomic<double *> g_scratch_addr[kMaxDevices] = {};
 
-__global__ void k_nmd_nodes(int nn, int ne, const int *__restrict__ sup_off, const int *__restrict__ sup_ent,
+__global__ void k_nmd_nodes(int nn, const int *__restrict__ sup_off, const int *__restrict__ sup_ent,
                             const double *__restrict__ dpressure, const double *__restrict__ volume,
                             const double *__restrict__ volume_n, double *__restrict__ dp_nd)
 {
@@ -53,6 +61,27 @@ __global__ void k_nmd_elems(int ne, int ndims, const int *__restrict__ conn, con
     for (int i = 0; i < ndims; ++i) stress[(size_t)i * ne + e] += (-dp_orig + dp_el) / ndims;   // :234
 }
 
+// Device address of the scratch on device dev (nullptr on failure).
+double *scratch_address(int dev, cudaStream_t s)
+{
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t qe = cudaStreamIsCapturing(s, &cap);
+    if (qe != cudaSuccess) {
+        // the legacy stream reports an error while another stream captures
+        // in global mode; the lookup is not allowed then either
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusActive;
+    }
+    if (cap != cudaStreamCaptureStatusNone) return g_scratch_addr[dev].load(std::memory_order_relaxed);
+    void *ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_nmd_scratch) != cudaSuccess || !ptr) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    g_scratch_addr[dev].store(static_cast<double *>(ptr), std::memory_order_relaxed);
+    return static_cast<double *>(ptr);
+}
+
 }  // namespace
 
 extern "C" int des_nmd_stress_noalloc(int ndims, int nnode, int nelem, const int *conn, const int *sup_off,
@@ -67,20 +96,24 @@ extern "C" int des_nmd_stress_noalloc(int ndims, int nnode, int nelem, const int
         return DES_EINPUT;
     }
     if (!conn || !sup_off || !sup_ent || !dpressure || !volume || !volume_n || !stress) return DES_EINPUT;
+    // An error left pending on this thread by earlier, unrelated work is the
+    // caller's: report it without consuming it, and launch nothing.
+    cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess) {
+        fprintf(stderr, "des_nmd_stress_noalloc: a CUDA error from earlier work is pending (%s); nothing launched\n",
+                cudaGetErrorString(pending));
+        return DES_ECUDA;
+    }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return DES_ECUDA;
-    if (!g_scratch_addr[dev]) {
-        // once per device, with that device current: the host-side symbol
-        // is only a stand-in, the kernels need the device address
-        void *ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, g_nmd_scratch);
-        if (e != cudaSuccess || !ptr) return DES_ECUDA;
-        g_scratch_addr[dev] = static_cast<double *>(ptr);
-    }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double *scratch = scratch_address(dev, s);
+    if (!scratch) return DES_ECUDA;
     const int tpb = 256;
-    k_nmd_nodes<<<(nnode + tpb - 1) / tpb, tpb, 0, s>>>(nnode, nelem, sup_off, sup_ent, dpressure, volume,
-                                                         volume_n, g_scratch_addr[dev]);
-    k_nmd_elems<<<(nelem + tpb - 1) / tpb, tpb, 0, s>>>(nelem, ndims, conn, dpressure, g_scratch_addr[dev], stress);
-    return cudaGetLastError() == cudaSuccess ? DES_OK : DES_ECUDA;
+    k_nmd_nodes<<<(nnode + tpb - 1) / tpb, tpb, 0, s>>>(nnode, sup_off, sup_ent, dpressure, volume, volume_n,
+                                                         scratch);
+    if (cudaGetLastError() != cudaSuccess) return DES_ECUDA;
+    k_nmd_elems<<<(nelem + tpb - 1) / tpb, tpb, 0, s>>>(nelem, ndims, conn, dpressure, scratch, stress);
+    if (cudaGetLastError() != cudaSuccess) return DES_ECUDA;
+    return DES_OK;
 }
