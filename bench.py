@@ -22,10 +22,12 @@ Metric: Mtet-steps/s = nelem x steps / time (higher is better).
            fp64_pipe: its FP64 instructions per element (from the committed
            ncu capture) per second against 2 per SM per clock, the roof that
            binds on GB300;
-* cpu_baseline: the oracle (C restatement of the reference, OpenMP with the
-           reference's two-colour band scatter) on this host's cores, on a
-           bounded sample of the same workload.
---impl reference times that CPU implementation alone on the same workload.
+* cpu_baseline: the reference's own step (its fields/geometry/rheology/bc/
+           matprops objects compiled -O2 -fopenmp from its staged sources,
+           oracle/_ref) on this host's cores, at all threads and at one
+           thread, on a bounded sample of the same workload, with the oracle
+           (C restatement) beside it;
+--impl reference times the reference's OpenMP step alone on the same workload.
 With --gpus N > 1 (torchrun) every rank runs an independent replica
 (the path has no data-path exchange on one GPU per replica): "weak" scaling.
 """
@@ -146,7 +148,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(wl, st, cp, clock, nthreads, budget_s=12.0):
+def port_baseline(wl, st, cp, clock, nthreads, budget_s=12.0):
     """Oracle (CPU restatement, OpenMP) on the same workload: a bounded
     number of steps sized to ~budget_s seconds."""
     from oracle.oracle import Oracle, state_copy
@@ -167,6 +169,50 @@ def cpu_baseline(wl, st, cp, clock, nthreads, budget_s=12.0):
                       f"OpenMP x{nthreads} (two-colour element bands), {dt:.1f} s"}
 
 
+def reference_cpu():
+    """The reference's own step compiled with OpenMP (oracle/_ref), or None
+    where its sources are not staged."""
+    from oracle.oracle import Reference, reference_sources_available
+    if not reference_sources_available():
+        return None
+    try:
+        return Reference(3, flavour="omp")
+    except OSError:
+        return None
+
+
+def reference_timed(ref, wl, st, cp, clock, nthreads, budget_s):
+    """The reference's loop body (dynearthsol.cxx:325-361, its own fields,
+    geometry, rheology, bc and matprops objects built -O2 -fopenmp) on
+    nthreads OpenMP threads, for a number of steps sized to ~budget_s
+    seconds: (Mtet-steps/s, steps, seconds of the loop alone)."""
+    from oracle.oracle import state_copy
+    ref.set_threads(nthreads)
+    _, t_cal = ref.run_timed(wl, state_copy(st), cp, clock, 1)
+    nsteps = int(max(2, min(200, budget_s / max(t_cal, 1e-6))))
+    _, sec = ref.run_timed(wl, state_copy(st), cp, clock, nsteps)
+    return wl.mesh.nelem * nsteps / sec / 1e6, nsteps, sec
+
+
+def cpu_baseline(wl, st, cp, clock, nthreads, budget_s=12.0):
+    """The reference's own OpenMP step on this host's cores (kind
+    "reference"), at all threads and at 1 thread, with the oracle port beside
+    it; the port alone where the reference's sources are not staged."""
+    port = port_baseline(wl, st, cp, clock, nthreads, budget_s)
+    ref = reference_cpu()
+    if ref is None:
+        return port
+    v, n, sec = reference_timed(ref, wl, st, cp, clock, nthreads, budget_s)
+    v1, n1, sec1 = reference_timed(ref, wl, st, cp, clock, 1, budget_s)
+    ref.set_threads(nthreads)
+    return {"value": v, "unit": "Mtet-steps/s", "cores": nthreads, "kind": "reference",
+            "sample": f"{n} steps of the full {wl.mesh.nelem:,}-tet workload through the reference's own "
+                      f"fields/geometry/rheology/bc/matprops objects (-O2 -fopenmp, {2 * nthreads} element "
+                      f"bands), OpenMP x{nthreads}, {sec:.1f} s of loop",
+            "one_thread": {"value": v1, "cores": 1, "sample": f"{n1} steps, {sec1:.1f} s of loop"},
+            "port": port}
+
+
 def setup_workload(name):
     from dynearthsol_gb300.config import initial_state, make_workload
     wl = make_workload(name)
@@ -175,23 +221,36 @@ def setup_workload(name):
 
 
 def run_reference(args, rank, world):
-    """CPU implementation (oracle port) on this host, all threads."""
+    """The reference's own CPU implementation of the step on this host, all
+    threads: its fields/geometry/rheology/bc/matprops objects compiled with
+    OpenMP from its staged sources (oracle/_ref); the oracle port where those
+    are not staged."""
     if rank != 0:
         return 0
     wl, st, cp = setup_workload(args.workload)
-    from oracle.oracle import Oracle
+    from oracle.oracle import Oracle, state_copy
     nthreads = os.cpu_count() or 1
     o = Oracle(wl, st, cp, nthreads)
     o.init_fields()
     clock = o.clock
-    for _ in range(args.warmup):
-        o.run(1)
-    # each timed step is one explicit step of the full workload
-    t0 = time.perf_counter()
-    rc = o.run(args.steps)
-    el = time.perf_counter() - t0
-    if rc:
-        raise RuntimeError(f"oracle failed ({rc})")
+    ref = reference_cpu()
+    if ref is not None:
+        ref.set_threads(nthreads)
+        s = state_copy(st)
+        clock, _ = ref.run_timed(wl, s, cp, clock, args.warmup)
+        # each timed step is one explicit step of the full workload
+        _, el = ref.run_timed(wl, s, cp, clock, args.steps)
+        kind, what = "reference", (f"the reference's own objects (-O2 -fopenmp, {2 * nthreads} element bands), "
+                                   "loop time only")
+    else:
+        for _ in range(args.warmup):
+            o.run(1)
+        t0 = time.perf_counter()
+        rc = o.run(args.steps)
+        el = time.perf_counter() - t0
+        if rc:
+            raise RuntimeError(f"oracle failed ({rc})")
+        kind, what = "port", "the oracle port (the reference's sources are not staged here)"
     v = wl.mesh.nelem * args.steps / el / 1e6
     line = {
         "impl": "reference", "metric": metric_name(args), "value": v, "unit": "Mtet-steps/s",
@@ -199,9 +258,9 @@ def run_reference(args, rank, world):
         "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_of(args, wl),
-        "cpu_baseline": {"value": v, "unit": "Mtet-steps/s", "cores": nthreads, "kind": "port",
+        "cpu_baseline": {"value": v, "unit": "Mtet-steps/s", "cores": nthreads, "kind": kind,
                          "sample": f"{args.steps} timed steps (after {args.warmup} warm-up) of the full "
-                                   f"{wl.mesh.nelem:,}-tet workload, OpenMP x{nthreads}"},
+                                   f"{wl.mesh.nelem:,}-tet workload, OpenMP x{nthreads}: {what}"},
         "e2e": {"value": v, "unit": "Mtet-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -320,11 +379,13 @@ def main():
                     help="steps of the damping-2 mixed-vs-FP64 stress-error gate (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=500,
                     help="window of the adjoint benchmark (0: skip it)")
-    ap.add_argument("--adjoint-every", type=int, default=0,
+    ap.add_argument("--adjoint-every", type=int, default=50,
                     help="checkpoint spacing of the adjoint window (0: the whole window as one segment, taped by "
                          "its forward, or every 50 steps when that tape does not fit in device memory)")
-    ap.add_argument("--adjoint-fd", type=int, default=4,
+    ap.add_argument("--adjoint-fd", type=int, default=20,
                     help="elements checked against central differences in the adjoint benchmark")
+    ap.add_argument("--yield-adjoint-steps", type=int, default=100,
+                    help="window of the adjoint with yielding elements (cohesion and friction gradients; 0: skip)")
     ap.add_argument("--heat-adjoint-steps", type=int, default=200,
                     help="window of the heat adjoint on the 4,056,000-tet jittered mesh (0: skip)")
     ap.add_argument("--scale-steps", type=int, default=1000,
@@ -423,6 +484,9 @@ def main():
     adjoint = None
     if args.adjoint_steps > 0 and rank == 0:
         adjoint = adjoint_bench(args, stream)
+    yield_adjoint = None
+    if args.yield_adjoint_steps > 0 and rank == 0:
+        yield_adjoint = yield_adjoint_bench(args, stream)
     heat_adjoint = None
     if args.heat_adjoint_steps > 0 and rank == 0:
         heat_adjoint = heat_adjoint_bench(args, stream)
@@ -444,6 +508,7 @@ def main():
             "mixed_error_gate": gate,
             "e2e": e2e,
             "adjoint": adjoint,
+            "yield_adjoint": yield_adjoint,
             "heat_adjoint": heat_adjoint,
             "scale": scale,
             "gpu_launches": int(launches),
@@ -493,9 +558,10 @@ def adjoint_bench(args, stream):
     log10 viscosity, ~1e-3 per element) carries the whole gradient's signal."""
     import torch
     from dynearthsol_gb300 import capi
-    from dynearthsol_gb300.adjoint import Window, adjoint_workload, fd5, surface_velocity_misfit, top_nodes
+    from dynearthsol_gb300.adjoint import Window, adjoint_workload, surface_velocity_misfit, top_nodes
     from dynearthsol_gb300.config import initial_state
     from dynearthsol_gb300.solver import DeviceModel
+    from dynearthsol_gb300.adjoint import fd5_misfit
     K = args.adjoint_steps
     C = args.adjoint_every if args.adjoint_every > 0 else K
     wl, lv_t, lv_s = adjoint_workload()
@@ -509,9 +575,6 @@ def adjoint_bench(args, stream):
     # the whole window as one segment when its tape fits, else every 50 steps
     target = run_fitting_tape(win, {LV: lv_t}, [C] if C < K else [K, 50])["vel"]
     C = win.C
-
-    def loss_of(lv):
-        return surface_velocity_misfit(win.run({LV: lv})["vel"], target, nodes)[0]
 
     # timed forward (recording checkpoints) and reverse sweep
     win.set_params({LV: lv_s})
@@ -540,25 +603,37 @@ def adjoint_bench(args, stream):
     rng = np.random.default_rng(2024)
     cand = np.nonzero(np.abs(g) >= 0.01 * np.abs(g).max())[0]
     fd = []
+    # each difference L(+) - L(-) is formed from the two runs' velocities
+    # (misfit_difference), not as the difference of two nearly equal misfits
     for e in rng.choice(cand, size=min(args.adjoint_fd, len(cand)), replace=False):
-        def along(t, e=e):
+        def vel_at(t, e=e):
             lv = lv_s.copy()
             lv[e] += t
-            return loss_of(lv)
-        d = fd5(along, 1e-2)
+            return win.run_vel({LV: lv})
+        d = fd5_misfit(vel_at, 1e-2, target, nodes)
         fd.append({"elem": int(e), "adjoint": float(g[e]), "central_fd": float(d),
                    "rel_err": float(abs(d - g[e]) / max(abs(d), abs(g[e]), 1e-300))})
     # directional derivative along the normalised gradient: the whole
     # gradient's signal, well above the rounding of the misfit
     gn = np.linalg.norm(g)
     ghat = g / gn
-
-    def along_g(t):
-        return loss_of(lv_s + t * ghat)
-
-    dfd = fd5(along_g, 1.0)
+    dfd = fd5_misfit(lambda t: win.run_vel({LV: lv_s + t * ghat}), 1.0, target, nodes)
     gdir = {"step": 1.0, "adjoint": float(gn), "central_fd": float(dfd),
             "rel_err": float(abs(dfd - gn) / max(abs(dfd), gn))}
+    # the extension velocities of the two x boundaries
+    vbc0 = win.base_vbc.copy()
+    vbc_fd = []
+    for i in (0, 1):
+        h = 1e-2 * abs(vbc0[i])
+        def vel_vbc(t, i=i):
+            v = vbc0.copy()
+            v[i] += t
+            return win.run_vel({LV: lv_s, "vbc_values": v})
+        d = fd5_misfit(vel_vbc, h, target, nodes)
+        a = float(grad["vbc_values"][i])
+        vbc_fd.append({"boundary": ["x0", "x1"][i], "adjoint": a, "central_fd": float(d),
+                       "rel_err": float(abs(d - a) / max(abs(d), abs(a), 1e-300))})
+    win.set_params({"vbc_values": vbc0})
     m.close()
     return {"workload": "c3_3d_adjoint", "nelem": wl.mesh.nelem, "window_steps": K, "checkpoint_every": C,
             "mode": ("one segment, taped by the forward (no recompute)" if C >= K
@@ -568,10 +643,86 @@ def adjoint_bench(args, stream):
             "forward_and_adjoint_over_graph_step": (t_fwd + t_bwd) / t_step,
             "gradients": "log10 viscosity, shear modulus, cohesion0/1, friction0/1 per element; vbc_values",
             "vbc_grad_x": [float(grad["vbc_values"][0]), float(grad["vbc_values"][1])],
+            "vbc_fd_check": vbc_fd,
             "fd_check": fd, "fd_max_rel_err": max((r["rel_err"] for r in fd), default=None),
+            "fd": "fourth-order central differences, each L(+) - L(-) formed from the velocities",
             "fd_gradient_direction": gdir,
             "dt": "held at the start value (compute_dt not called in the window)",
             "damping_option": 2}
+
+
+def yield_adjoint_bench(args, stream):
+    """The adjoint through yielding elements: the 3D workload's physics on
+    20x20x6 cubes (14,400 tets) with a band of weak material (per-element
+    cohesion and friction), damping option 2, run 1000 steps until the band
+    yields; then a window of K steps (checkpoint every K/5) whose loss is
+    the top-surface velocity misfit against a run with the band's cohesion1
+    perturbed by +-20 %.  The gradients with respect to cohesion0/1 and
+    friction0/1 are checked by fourth-order central differences at yielding
+    elements, and along the normalised cohesion1 gradient."""
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.adjoint import (Window, fd5_misfit, surface_velocity_misfit, top_nodes,
+                                           yielding_adjoint_workload)
+    from dynearthsol_gb300.config import initial_state
+    from dynearthsol_gb300.solver import DeviceModel
+    K = args.yield_adjoint_steps
+    C = max(1, K // 5)
+    wl, c1_t, c1_s = yielding_adjoint_workload()
+    st, cp = initial_state(wl)
+    m = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_FP64, stream=stream.cuda_stream)
+    init = m.init_fields(st)
+    m.step(1000)
+    start = m.download()
+    clock = m.clock()
+    win = Window(m, start, clock, K, C)
+    nodes = top_nodes(wl.mesh)
+    C1, C0, F0, F1 = capi.EF_COHESION1, capi.EF_COHESION0, capi.EF_FRICTION0, capi.EF_FRICTION1
+    target = win.run({C1: c1_t})["vel"]
+    win.set_params({C1: c1_s})
+    m.upload(win.start, clock)
+    m.sync()
+    t0 = time.perf_counter()
+    m.adjoint_forward(K, C)
+    m.sync()
+    t_fwd = time.perf_counter() - t0
+    fin = m.download()
+    yielding = np.nonzero(fin["plstrain"] > start["plstrain"] + 1e-12)[0]
+    loss, seed = surface_velocity_misfit(fin["vel"], target, nodes)
+    t0 = time.perf_counter()
+    _, grad = m.adjoint_backward({"vel": seed}, want_start=False)
+    m.sync()
+    t_bwd = time.perf_counter() - t0
+    base = {k: win.fields[k].copy() for k in (C0, C1, F0, F1)}
+    rng = np.random.default_rng(7)
+    checks = []
+    for key, name, h in ((C1, "cohesion1", 1e3), (C0, "cohesion0", 1e3), (F1, "friction1", 1e-2),
+                         (F0, "friction0", 1e-2)):
+        g = grad[key]
+        cand = yielding[np.abs(g[yielding]) >= 0.05 * np.abs(g[yielding]).max()] if len(yielding) else []
+        for e in (rng.choice(cand, size=min(5, len(cand)), replace=False) if len(cand) else []):
+            def vel_at(t, e=e, key=key):
+                p = dict(base)
+                p[key] = base[key].copy()
+                p[key][e] += t
+                return win.run_vel(p)
+            d = fd5_misfit(vel_at, h, target, nodes)
+            checks.append({"param": name, "elem": int(e), "adjoint": float(g[e]), "central_fd": float(d),
+                           "rel_err": float(abs(d - g[e]) / max(abs(d), abs(g[e]), 1e-300))})
+    g1 = grad[C1]
+    gn = float(np.linalg.norm(g1))
+    ghat = g1 / gn
+    p_dir = dict(base)
+    dfd = fd5_misfit(lambda t: win.run_vel({**p_dir, C1: base[C1] + t * 1e4 * ghat}), 1.0, target, nodes) / 1e4
+    m.close()
+    return {"workload": "3d yielding band (20x20x6 cubes x 6 = 14,400 tets, per-element cohesion/friction)",
+            "start_step": 1000, "window_steps": K, "checkpoint_every": C,
+            "yielded_elements_in_window": int(len(yielding)), "loss": loss,
+            "forward_s": t_fwd, "adjoint_s": t_bwd, "adjoint_over_forward": t_bwd / t_fwd,
+            "nonzero_gradients": {n: int((np.abs(grad[k]) > 0).sum()) for k, n in
+                                  ((C0, "cohesion0"), (C1, "cohesion1"), (F0, "friction0"), (F1, "friction1"))},
+            "fd_check": checks, "fd_max_rel_err": max((r["rel_err"] for r in checks), default=None),
+            "fd_cohesion1_direction": {"adjoint": gn, "central_fd": float(dfd),
+                                       "rel_err": float(abs(dfd - gn) / max(abs(dfd), gn))}}
 
 
 def scale_bench(args, stream):

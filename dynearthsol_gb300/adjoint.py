@@ -60,6 +60,13 @@ class Window:
         self.m.adjoint_forward(self.K, self.C)
         return self.m.download()
 
+    def run_vel(self, params: dict | None = None) -> np.ndarray:
+        """Forward window, as run(), returning the final velocities only."""
+        self.set_params(params)
+        self.m.upload(self.start, self.clock)
+        self.m.adjoint_forward(self.K, self.C)
+        return self.m.download_fields(("vel",))["vel"]
+
     def gradients(self, seed: dict):
         """Adjoint of the window last run: (start-state adjoint, parameter gradients)."""
         return self.m.adjoint_backward(seed)
@@ -149,6 +156,24 @@ def window_function():
     return WindowFunction
 
 
+def misfit_difference(vel_a: np.ndarray, vel_b: np.ndarray, target: np.ndarray, nodes: np.ndarray) -> float:
+    """L(a) - L(b) of the surface-velocity misfit, formed without subtracting
+    two nearly equal misfits: 1/2 sum (v_a - v_b)(v_a + v_b - 2 v_target)
+    over the nodes (exact algebra; only the velocity differences round)."""
+    va, vb, vt = vel_a[nodes], vel_b[nodes], target[nodes]
+    return 0.5 * float(np.sum((va - vb) * ((va - vt) + (vb - vt))))
+
+
+def fd5_misfit(vel_at, h: float, target: np.ndarray, nodes: np.ndarray) -> float:
+    """Fourth-order central difference of the misfit along a direction,
+    (8 (L(h) - L(-h)) - (L(2h) - L(-2h))) / 12h, each difference taken by
+    misfit_difference; vel_at(t) = the final velocities at step t."""
+    v = {t: vel_at(t) for t in (h, -h, 2 * h, -2 * h)}
+    d1 = misfit_difference(v[h], v[-h], target, nodes)
+    d2 = misfit_difference(v[2 * h], v[-2 * h], target, nodes)
+    return (8 * d1 - d2) / (12 * h)
+
+
 def surface_velocity_misfit(final_vel: np.ndarray, target: np.ndarray, nodes: np.ndarray):
     """L = 1/2 sum over the given nodes of |v - v_target|^2 and its seed."""
     r = final_vel[nodes] - target[nodes]
@@ -208,3 +233,28 @@ def adjoint_workload(cells=None, seed: int = 12345):
                       capi.EF_FRICTION0: np.full(ne, mt.friction_angle0[0]),
                       capi.EF_FRICTION1: np.full(ne, mt.friction_angle1[0])}
     return wl, lv_target, lv_start
+
+
+def yielding_adjoint_workload(cells=(20, 20, 6), halfwidth: float = 15e3, seed: int = 7):
+    """A window in which elements yield: the 3D workload's physics with
+    damping option 2 and, as per-element fields, a vertical band of weak
+    material (|x - xlength/2| < halfwidth: cohesion 1 -> 0.1 MPa, friction
+    10 -> 5 degrees) in which the Mohr-Coulomb return map is active after a
+    few hundred steps.  Returns (workload, target cohesion1, start cohesion1):
+    the target run perturbs the band's cohesion1 by a seeded +-20 %."""
+    from dataclasses import replace
+    from .config import elem_center, make_workload
+    wl = make_workload("c1_3d_evp", cells=cells, seed=seed)
+    wl.params = replace(wl.params, damping_option=2)
+    mt = wl.mat
+    band = np.abs(elem_center(wl.mesh)[:, 0] - 0.5 * wl.mesh.lengths[0]) < halfwidth
+    ne = wl.mesh.nelem
+    c0 = np.where(band, 1e6, mt.cohesion0[0])
+    c1 = np.where(band, 1e5, mt.cohesion1[0])
+    f0 = np.where(band, 10.0, mt.friction_angle0[0])
+    f1 = np.where(band, 5.0, mt.friction_angle1[0])
+    wl.elem_fields = {capi.EF_SHEAR_MODULUS: np.full(ne, mt.shear_modulus[0]), capi.EF_COHESION0: c0,
+                      capi.EF_COHESION1: c1, capi.EF_FRICTION0: f0, capi.EF_FRICTION1: f1}
+    rng = np.random.default_rng(seed)
+    c1_target = c1 * (1 + 0.2 * rng.uniform(-1, 1, ne) * band)
+    return wl, c1_target, c1

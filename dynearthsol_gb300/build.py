@@ -23,7 +23,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdesgpu.so")
 
 SOURCES = ["des_kernels.cu", "des_mixed.cu", "des_capi.cu", "des_noalloc.cu", "des_adjoint.cu",
-           "des_adjoint_host.cu", "des_output.cu"]
+           "des_adjoint_host.cu", "des_output.cu", "des_phase.cu", "des_topology.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off"]

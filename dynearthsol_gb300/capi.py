@@ -137,6 +137,19 @@ class DesHostState(C.Structure):
     ]
 
 
+class DesQualityParams(C.Structure):
+    """des_quality_params: the Param::mesh fields bad_mesh_quality reads."""
+    _fields_ = [("smallest_size", C.c_double), ("resolution", C.c_double), ("min_quality", C.c_double),
+                ("max_boundary_distortion", C.c_double), ("remeshing_option", C.c_int)]
+
+
+class DesTopology(C.Structure):
+    """des_topology: a mesh as remeshing leaves it (connectivity, boundary
+    flags, boundary segments and their flags)."""
+    _fields_ = [("ndims", C.c_int), ("nnode", C.c_int), ("nelem", C.c_int), ("connectivity", _ip),
+                ("bcflag", _up), ("nseg", C.c_int), ("segment", _ip), ("segflag", _ip)]
+
+
 class DesAdjointGrad(C.Structure):
     """des_adjoint_grad: per-element gradient arrays (NULL = skip) and the
     gradient with respect to each boundary's prescribed velocity value."""
@@ -216,6 +229,12 @@ _SIGS = {
     "des_compute_dt": [C.c_void_p, _dp],
     "des_update_mesh": [C.c_void_p],
     "des_worst_elem_quality": [C.c_void_p, _dp, _ip],
+    "des_bad_mesh_quality": [C.c_void_p, C.POINTER(DesQualityParams), _ip, _ip, _dp],
+    "des_set_markers": [C.c_void_p, C.c_int, _ip, _dp, _ip],
+    "des_build_topology": [C.POINTER(DesTopology), _ip, _ip, _ip, _ip, C.c_void_p],
+    "des_remesh": [C.c_void_p, C.POINTER(DesTopology), _ip],
+    "des_phase_changes": [C.c_void_p, C.c_int, _ip, _ip],
+    "des_get_markers": [C.c_void_p, _ip, _ip],
     "des_get_clock": [C.c_void_p, _dp, _dp, _ip],
     "des_set_clock": [C.c_void_p, C.c_double, C.c_double, C.c_int],
     "des_step": [C.c_void_p, C.c_int],
@@ -299,3 +318,51 @@ def read_save(path: str) -> dict:
         dt = np.int32 if name == "connectivity" else (np.uint32 if name == "bcflag" else np.float64)
         out[name] = np.frombuffer(raw[off:end], dtype=dt)
     return out
+
+
+def segments_of(mesh, order=None):
+    """Boundary segments of a mesh as a mesher lists them (Variables::segment,
+    segflag): the nodes of each boundary facet (NODE_OF_FACET,
+    constants.hpp:59-71) and its boundary's bit, in the mesh's boundary-facet
+    order or in the given order of those facets."""
+    from .mesh import NODE_OF_FACET_2D, NODE_OF_FACET_3D
+    nd = mesh.ndims
+    tab = NODE_OF_FACET_3D if nd == 3 else NODE_OF_FACET_2D
+    off = np.asarray(mesh.bfacet_offsets)
+    bdry = np.zeros(off[-1], dtype=np.int32)
+    for b in range(NBDRY):
+        bdry[off[b]:off[b + 1]] = b
+    fac = np.asarray(mesh.bfacets)
+    idx = np.arange(off[-1]) if order is None else np.asarray(order)
+    e, f = fac[idx, 0], fac[idx, 1]
+    seg = np.ascontiguousarray(np.asarray(mesh.connectivity)[e[:, None], tab[f]], dtype=np.int32)
+    flag = np.ascontiguousarray((1 << bdry[idx]).astype(np.int32))
+    return seg, flag
+
+
+class Topology:
+    """A DesTopology with the arrays it points to."""
+
+    def __init__(self, mesh, segment=None, segflag=None):
+        if segment is None:
+            segment, segflag = segments_of(mesh)
+        self.conn = np.ascontiguousarray(mesh.connectivity, dtype=np.int32)
+        self.bcflag = np.ascontiguousarray(mesh.bcflag, dtype=np.uint32)
+        self.segment = np.ascontiguousarray(segment, dtype=np.int32)
+        self.segflag = np.ascontiguousarray(segflag, dtype=np.int32)
+        self.struct = DesTopology(mesh.ndims, mesh.nnode, mesh.nelem, iptr(self.conn), uptr(self.bcflag),
+                                  self.segment.shape[0], iptr(self.segment), iptr(self.segflag))
+
+
+def build_topology(topo: "Topology", stream=None):
+    """des_build_topology: (sup_off, sup_elem, bfacet_offsets, bfacets)."""
+    lib = load_library()
+    t = topo.struct
+    off = np.zeros(t.nnode + 1, np.int32)
+    elems = np.zeros(t.nelem * (t.ndims + 1), np.int32)
+    boff = np.zeros(NBDRY + 1, np.int32)
+    fac = np.zeros((max(t.nseg, 1), 2), np.int32)
+    rc = lib.des_build_topology(C.byref(t), iptr(off), iptr(elems), iptr(boff), iptr(fac), stream)
+    if rc:
+        raise DesError(rc, "des_build_topology failed")
+    return off, elems, boff, fac[:boff[-1]]

@@ -213,8 +213,16 @@ int des_last_error(const des_ctx *c, char *buf, size_t len)
     return DES_OK;
 }
 
-int des_create(const des_mesh *mesh, const des_params *param, const des_material *mat, int precision,
-               void *stream, des_ctx **out)
+}  // extern "C"
+
+namespace des {
+
+// des_create with, optionally, the support lists already built (CSR offsets
+// and entries element * 4 + local node, ascending element: des_remesh
+// builds them on the device)
+int create_context(const des_mesh *mesh, const des_params *param, const des_material *mat, int precision,
+                   cudaStream_t stream, const std::vector<int> *pre_off, const std::vector<int> *pre_ent,
+                   des_ctx **out)
 {
     des_ctx *c = nullptr;
     if (!out) return fail_msg(g_create_error, DES_EINPUT, "out is NULL");
@@ -257,10 +265,15 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
         }
     }
     // support lists in ascending element order (create_support, mesh.cxx:1707-1721)
-    std::vector<int> sup_off(nn + 1, 0), sup_ent((size_t)ne * npe);
-    for (long long i = 0; i < (long long)ne * npe; ++i) sup_off[cn[i] + 1]++;
-    for (int n = 0; n < nn; ++n) sup_off[n + 1] += sup_off[n];
-    {
+    std::vector<int> sup_off, sup_ent;
+    if (pre_off && pre_ent && pre_off->size() == (size_t)nn + 1 && pre_ent->size() == (size_t)ne * npe) {
+        sup_off = *pre_off;
+        sup_ent = *pre_ent;
+    } else {
+        sup_off.assign(nn + 1, 0);
+        sup_ent.resize((size_t)ne * npe);
+        for (long long i = 0; i < (long long)ne * npe; ++i) sup_off[cn[i] + 1]++;
+        for (int n = 0; n < nn; ++n) sup_off[n + 1] += sup_off[n];
         std::vector<int> fill(sup_off.begin(), sup_off.end() - 1);
         for (int e = 0; e < ne; ++e)
             for (int i = 0; i < npe; ++i) sup_ent[fill[cn[(size_t)e * npe + i]]++] = e * 4 + i;
@@ -398,7 +411,7 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     add((void **)&p.fv, (size_t)std::max(nbf, 1) * nd * D);
     add((void **)&p.clk, sizeof(Clock));
     add((void **)&p.err, sizeof(unsigned));
-    add((void **)&c->d_red, 2 * sizeof(unsigned long long));
+    add((void **)&c->d_red, 4 * sizeof(unsigned long long));
     c->stage_doubles = std::max((size_t)ne * std::max(c->nstr, npe), (size_t)nn * nd);
     add((void **)&c->d_stage, c->stage_doubles * D);
     size_t total = 0;
@@ -530,12 +543,27 @@ int des_create(const des_mesh *mesh, const des_params *param, const des_material
     return DES_OK;
 }
 
-int des_destroy(des_ctx *c)
+}  // namespace des
+
+extern "C" {
+
+int des_create(const des_mesh *mesh, const des_params *param, const des_material *mat, int precision,
+               void *stream, des_ctx **out)
 {
-    if (!c) return DES_OK;
+    return create_context(mesh, param, mat, precision, static_cast<cudaStream_t>(stream), nullptr, nullptr, out);
+}
+
+}  // extern "C"
+
+namespace des {
+
+// every device resource of c except its stream; c itself is not deleted
+void release_context(des_ctx *c)
+{
     cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
     adj_free(c);
+    markers_free(c);
     if (c->ystream) {
         cudaStreamSynchronize(c->ystream);
         cudaStreamDestroy(c->ystream);
@@ -552,6 +580,17 @@ int des_destroy(des_ctx *c)
     for (int k = 0; k < DES_EF_COUNT; ++k)
         if (c->d_ef[k]) cudaFree(c->d_ef[k]);
     cudaFree(c->pool);
+    c->pool = nullptr;
+}
+
+}  // namespace des
+
+extern "C" {
+
+int des_destroy(des_ctx *c)
+{
+    if (!c) return DES_OK;
+    release_context(c);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return DES_OK;
@@ -1087,6 +1126,58 @@ int des_worst_elem_quality(des_ctx *c, double *quality, int *elem)
     }
     if (quality) *quality = q;
     if (elem) *elem = w;
+    return DES_OK;
+}
+
+int des_bad_mesh_quality(des_ctx *c, const des_quality_params *qp, int *code, int *index, double *value)
+{
+    if (!c || !qp || !code || !index) return DES_EINPUT;
+    const int nd = c->kp.nd;
+    // the volume of the equilateral triangle / tetrahedron of unit side
+    // (remeshing.cxx:76-82), and the thresholds as the reference forms them
+    const double sizefactor = nd == 3 ? 0.118 : 0.433;
+    const double smallest_vol = qp->smallest_size * sizefactor * std::pow(qp->resolution, nd);
+    const double bottom = -c->kp.prm.zlength;
+    const double dist = qp->max_boundary_distortion * qp->resolution;
+    const int opt = qp->remeshing_option;
+    const int check_bottom = (opt == 1 || opt == 2 || opt == 11);
+    unsigned long long init[4] = {~0ull, ~0ull, ~0ull, ~0ull}, res[4];
+    CK(cudaMemcpyAsync(c->d_red, init, sizeof init, cudaMemcpyHostToDevice, c->stream));
+    int rc = check_launch(c, launch_quality_scans(c->kp, c->stream, smallest_vol, bottom, dist, check_bottom,
+                                                  c->d_red) +
+                                 launch_quality(c->kp, c->stream, c->d_red));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(res, c->d_red, sizeof res, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (res[2] != ~0ull) {
+        *code = 3;
+        *index = (int)res[2];
+        if (value) CK(cudaMemcpy(value, c->kp.vol + res[2], sizeof(double), cudaMemcpyDeviceToHost));
+        return DES_OK;
+    }
+    if (check_bottom && res[3] != ~0ull) {
+        *code = 2;
+        *index = (int)res[3];
+        if (value)
+            CK(cudaMemcpy(value, c->kp.x + (size_t)(nd - 1) * c->kp.nn + res[3], sizeof(double),
+                          cudaMemcpyDeviceToHost));
+        return DES_OK;
+    }
+    double q;
+    memcpy(&q, &res[0], sizeof q);
+    int w = (int)res[1];
+    if (!(q < 1)) {   // worst_elem_quality starts from q = 1, worst = 0
+        q = 1;
+        w = 0;
+    }
+    if (nd == 3) q = std::pow(q, 1.0 / 3);   // remeshing.cxx:1924-1927
+    if (q < qp->min_quality) {
+        *code = 1;
+        *index = w;
+        if (value) *value = q;
+        return DES_OK;
+    }
+    *code = 0;
     return DES_OK;
 }
 

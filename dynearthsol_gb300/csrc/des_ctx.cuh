@@ -58,6 +58,10 @@ struct des_ctx {
     std::string err;
     bool has_state = false;
     des::AdjWork *adj = nullptr;  // reverse-mode workspace, created on first use
+    // markers on the device (des_set_markers): one block of element ids,
+    // material types, hydrous counts and barycentric coordinates
+    int nmarkers = 0;
+    void *d_markers = nullptr;
 };
 
 namespace des {
@@ -72,5 +76,17 @@ int ctx_put_field(des_ctx *c, const double *host, double *dev, int n, int ncomp)
 int ctx_get_field(des_ctx *c, const double *dev, double *host, int n, int ncomp);
 // frees the reverse-mode workspace (des_adjoint_host.cu)
 void adj_free(des_ctx *c);
+// frees the device markers (des_phase.cu)
+void markers_free(des_ctx *c);
+// des_create with optionally pre-built support lists (des_capi.cu)
+int create_context(const des_mesh *mesh, const des_params *param, const des_material *mat, int precision,
+                   cudaStream_t stream, const std::vector<int> *pre_off, const std::vector<int> *pre_ent,
+                   des_ctx **out);
+// every device resource of a context except its stream (des_capi.cu)
+void release_context(des_ctx *c);
+// support and boundary facet lists of a topology built on the device (des_topology.cu)
+int build_topology_device(const des_topology *t, cudaStream_t s, std::vector<int> &sup_off,
+                          std::vector<int> &sup_ent, std::vector<int> &bf_off, std::vector<int> &bf,
+                          std::string &err);
 
 }  // namespace des

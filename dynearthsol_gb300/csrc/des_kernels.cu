@@ -991,6 +991,31 @@ __global__ void __launch_bounds__(TPB) k_quality_arg(KP p, unsigned long long *r
     if (b == red[0]) atomicMin(&red[1], (unsigned long long)e);
 }
 
+// bad_mesh_quality's index scans (remeshing.cxx:1892-1919), one thread per
+// element and node: red[2] = the first element whose volume is below
+// smallest_vol, red[3] (check_bottom) = the first bottom node whose depth is
+// farther than dist from z = bottom.  Each warp takes the smallest candidate
+// index before one atomicMin, so the result is the first index whatever the
+// order the blocks run in.
+template <int ND>
+__global__ void __launch_bounds__(TPB) k_quality_scans(KP p, double smallest_vol, double bottom, double dist,
+                                                       int check_bottom, unsigned long long *red)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned small = 0xffffffffu, far = 0xffffffffu;
+    if (i < p.ne && p.vol[i] < smallest_vol) small = (unsigned)i;
+    if (check_bottom && i < p.nn && (p.bcflag[i] & BOUNDZ0)) {
+        const double z = p.x[(size_t)(ND - 1) * p.nn + i];
+        if (fabs(z - bottom) > dist) far = (unsigned)i;
+    }
+    small = __reduce_min_sync(0xffffffffu, small);
+    far = __reduce_min_sync(0xffffffffu, far);
+    if ((threadIdx.x & 31) == 0) {
+        if (small != 0xffffffffu) atomicMin(&red[2], (unsigned long long)small);
+        if (far != 0xffffffffu) atomicMin(&red[3], (unsigned long long)far);
+    }
+}
+
 // ==================================================================
 // material constants (see MatC): out[0..] = visc_coef[nmat], then for each
 // of the 2*nmat plastic table entries anphi, anpsi, sqrt(anphi), tan(phi)
@@ -1227,6 +1252,13 @@ int launch_quality(const KP &p, cudaStream_t s, unsigned long long *red)
     DISPATCH(k_quality_min, nblocks(p.ne), p, red);
     DISPATCH(k_quality_arg, nblocks(p.ne), p, red);
     return 2;
+}
+
+int launch_quality_scans(const KP &p, cudaStream_t s, double smallest_vol, double bottom, double dist,
+                         int check_bottom, unsigned long long *red)
+{
+    DISPATCH(k_quality_scans, nblocks(std::max(p.ne, p.nn)), p, smallest_vol, bottom, dist, check_bottom, red);
+    return 1;
 }
 
 __global__ void k_f64_to_f32(const double *__restrict__ a, float *__restrict__ b, long long n)

@@ -45,6 +45,9 @@ int launch_mass(const KP &p, cudaStream_t s);
 int launch_mass_sum(const KP &p, cudaStream_t s);
 int launch_dt_finalize(const KP &p, cudaStream_t s, bool only_on_step);
 int launch_quality(const KP &p, cudaStream_t s, unsigned long long *red);
+// red[2], red[3]: bad_mesh_quality's first tiny element and first drifted bottom node
+int launch_quality_scans(const KP &p, cudaStream_t s, double smallest_vol, double bottom, double dist,
+                         int check_bottom, unsigned long long *red);
 // out[4][ne]: density, mesh quality, viscosity, material of an output frame
 int launch_output_elem(const KP &p, double *out, cudaStream_t s);
 int launch_dt_reset(const KP &p, cudaStream_t s);

@@ -41,6 +41,7 @@
 #include "fields.hpp"
 #include "geometry.hpp"
 #include "rheology.hpp"
+#include "remeshing.hpp"
 
 #include "desgpu.h"
 
@@ -56,6 +57,10 @@ struct Shim {
     Variables *var = nullptr;
     des_ctx *ctx = nullptr;
     bool resident = false;
+    // host arrays of volume and volume_old as the device last saw them: the
+    // main loop swaps the two pointers (dynearthsol.cxx:226) before
+    // compute_volume, which the device mirrors in resident mode
+    const double *vol_seen = nullptr, *vol_old_seen = nullptr;
     double bn_cache[nbdrytypes][NDIMS];
     // storage the C structs point into
     std::vector<int> bfacet_off, bfacets, emark;
@@ -189,6 +194,8 @@ void create_ctx()
     fill_material(*g.param, v);
     int rc = des_create(&g.mesh, &g.prm, &g.mat, DES_PREC_FP64, nullptr, &g.ctx);
     if (rc) die(rc);
+    g.vol_seen = v.volume->data();
+    g.vol_old_seen = v.volume_old->data();
 }
 
 // host view of the current Variables arrays (pointers re-read every call:
@@ -284,6 +291,8 @@ void desgpu_shim_sync_to_device(void)
     if (!g.var) return;
     des_host_state s = view();
     check(des_upload_fields(ctx(), &s, DES_F_ALL));
+    g.vol_seen = g.var->volume->data();
+    g.vol_old_seen = g.var->volume_old->data();
 }
 
 }  // extern "C"
@@ -421,7 +430,13 @@ double dist2(const double *a, const double *b)   // geometry.cxx:16-24
 void compute_volume(const array_t &, const conn_t &, double_vec &)
 {
     up(DES_F_COORD);
-    check(des_compute_volume(ctx()));
+    des_ctx *c = ctx();
+    const double *vol = g.var->volume->data(), *vol_old = g.var->volume_old->data();
+    if (g.resident && vol == g.vol_old_seen && vol_old == g.vol_seen)
+        check(des_swap_volume(c));   // the host swapped volume and volume_old: keep the old volume
+    g.vol_seen = vol;
+    g.vol_old_seen = vol_old;
+    check(des_compute_volume(c));
     down(DES_F_VOLUME);
 }
 
@@ -530,4 +545,28 @@ void update_stress(const Variables &, tensor_t &, double_vec &, double_vec &, te
     check(des_update_stress(ctx()));
     down(DES_F_STRESS | DES_F_STRAIN | DES_F_STRAIN_RATE | DES_F_PLSTRAIN | DES_F_DELTA_PLSTRAIN |
          DES_F_STRESSYY | DES_F_DPRESSURE);
+}
+
+// ---------------------------------------------------------------------
+// remeshing.hpp: the quality check (remeshing.cxx:1882-1935) on the device.
+// remeshing.o defines this function too; the build weakens remeshing.o's
+// copy (objcopy --weaken-symbol) so that this one is linked.
+// ---------------------------------------------------------------------
+int bad_mesh_quality(const Param &param, const Variables &, int &index)
+{
+    up(DES_F_COORD | DES_F_VOLUME);
+    des_quality_params qp;
+    qp.smallest_size = param.mesh.smallest_size;
+    qp.resolution = param.mesh.resolution;
+    qp.min_quality = param.mesh.min_quality;
+    qp.max_boundary_distortion = param.mesh.max_boundary_distortion;
+    qp.remeshing_option = param.mesh.remeshing_option;
+    int code = 0, idx = index;
+    double value = 0;
+    check(des_bad_mesh_quality(ctx(), &qp, &code, &idx, &value));
+    if (code == 3) std::cout << "    The size of element #" << idx << " is too small.\n";
+    else if (code == 2) std::cout << "    Node #" << idx << " is too far from the bottm: z = " << value << "\n";
+    else if (code == 1) std::cout << "    Element #" << idx << " has mesh quality = " << value << ".\n";
+    if (code) index = idx;
+    return code;
 }

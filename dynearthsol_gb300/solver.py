@@ -88,6 +88,18 @@ class DeviceModel:
         self._check(self.lib.des_download_state(self.ctx, C.byref(hs)))
         return st
 
+    def download_fields(self, names) -> dict:
+        """Only the named state arrays (des_download_fields)."""
+        m = self.wl.mesh
+        full = empty_state(m.ndims, m.nnode, m.nelem)
+        st = {k: full[k] for k in names}
+        mask = 0
+        for k in names:
+            mask |= capi.F_SHP if k.startswith("shp") else capi.F_BITS[k]
+        hs = capi.host_state_struct(st)
+        self._check(self.lib.des_download_fields(self.ctx, C.byref(hs), mask))
+        return st
+
     def clock(self):
         t, dt, s = C.c_double(), C.c_double(), C.c_int()
         self._check(self.lib.des_get_clock(self.ctx, C.byref(t), C.byref(dt), C.byref(s)))
@@ -136,6 +148,55 @@ class DeviceModel:
             self._check(self.lib.des_worst_elem_quality(self.ctx, C.byref(q), C.byref(w)))
             return q.value, w.value
         self._check(getattr(self.lib, "des_" + name)(self.ctx))
+
+    def bad_mesh_quality(self, smallest_size, resolution, min_quality, max_boundary_distortion,
+                         remeshing_option):
+        """bad_mesh_quality (remeshing.cxx:1882-1935) on the device: (code,
+        index, value); index and value are None when the code is 0."""
+        qp = capi.DesQualityParams(smallest_size, resolution, min_quality, max_boundary_distortion,
+                                   remeshing_option)
+        code, idx, val = C.c_int(), C.c_int(-1), C.c_double()
+        self._check(self.lib.des_bad_mesh_quality(self.ctx, C.byref(qp), C.byref(code), C.byref(idx),
+                                                  C.byref(val)))
+        if code.value == 0:
+            return 0, None, None
+        return code.value, idx.value, val.value
+
+    # -- remeshing --
+    def remesh(self, wl: Workload, topology=None):
+        """des_remesh: the context's mesh becomes wl's (support lists and
+        boundary facets built on the device from its segments); upload the
+        state afterwards."""
+        topo = topology or capi.Topology(wl.mesh)
+        em = None if wl.mat.elemmarkers is None else np.ascontiguousarray(wl.mat.elemmarkers, dtype=np.int32)
+        self._topo = topo
+        self._check(self.lib.des_remesh(self.ctx, C.byref(topo.struct), capi.iptr(em)))
+        self.wl = wl
+        self.cs = CStructs(wl, self.comp_pressure)
+        self._ef = {}
+
+    # -- markers and phase changes --
+    def set_markers(self, elem: np.ndarray, eta: np.ndarray, mattype: np.ndarray):
+        """Markers (element, barycentric eta [n][ndims+1], material type) to the device."""
+        self._markers = (np.ascontiguousarray(elem, dtype=np.int32), np.ascontiguousarray(eta, dtype=np.float64),
+                         np.ascontiguousarray(mattype, dtype=np.int32))
+        e, t, m = self._markers
+        self._check(self.lib.des_set_markers(self.ctx, e.shape[0], capi.iptr(e), capi.dptr(t), capi.iptr(m)))
+
+    def phase_changes(self, option: int, hydrous: np.ndarray | None = None) -> int:
+        """phase_changes on the device; returns the number of markers changed."""
+        h = None if hydrous is None else np.ascontiguousarray(hydrous, dtype=np.int32)
+        n = C.c_int()
+        self._check(self.lib.des_phase_changes(self.ctx, option, capi.iptr(h), C.byref(n)))
+        return n.value
+
+    def get_markers(self):
+        """(material types [nmarkers], marker counts [nelem][nmat]) from the device."""
+        nm = self._markers[0].shape[0] if getattr(self, "_markers", None) else 0
+        mt = np.zeros(nm, np.int32)
+        em = np.zeros((self.wl.mesh.nelem, self.wl.mat.nmat), np.int32)
+        self._check(self.lib.des_get_markers(self.ctx, capi.iptr(mt), capi.iptr(em)))
+        return mt, em
 
     def sync(self):
         self._check(self.lib.des_synchronize(self.ctx))

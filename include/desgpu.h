@@ -217,6 +217,36 @@ int des_download_fields(des_ctx *ctx, des_host_state *st, unsigned mask);
  * (phasechanges.cxx:232-258) or marker remapping. */
 int des_set_elemmarkers(des_ctx *ctx, const int *elemmarkers);
 
+/* ---- markers and phase changes -----------------------------------------
+ * The markers of a multi-material context on the device (MarkerSet,
+ * markerset.hpp:11-84): for each marker its element, its barycentric
+ * coordinates eta[ndims+1] ([nmarkers][ndims+1], the reference's layout) and
+ * its material type.  Copied once after the host creates or remaps them
+ * (markerset.cxx:35-64; remap_markers after remeshing); replaces the
+ * previous set.  The context's per-element marker counts are not changed:
+ * they are set at des_create or by des_set_elemmarkers. */
+int des_set_markers(des_ctx *ctx, int nmarkers, const int *elem, const double *eta, const int *mattype);
+
+/* phase_changes (phasechanges.cxx:232-258) on the device, on the markers of
+ * des_set_markers: each marker's depth and temperature are interpolated from
+ * the device's coordinates and temperatures (PhaseChange::get_ZPT,
+ * phasechanges.cxx:24-39), its reference pressure follows, and the rule of
+ * phase_change_option decides its new material type: 1 = SimpleSubduction
+ * (phasechanges.cxx:44-160), 101 = the custom template (no change), 0 or a
+ * one-material context = nothing (phase_changes_init, phasechanges.cxx:
+ * 208-229).  A marker that changes moves from one material's count to the
+ * other's in the element's marker counts, so the next step blends the
+ * element's properties from the new counts.  hydrous_elemmarkers ([nelem],
+ * Variables::hydrous_elemmarkers; NULL = none) is read by the mantle ->
+ * serpentinite rule; hydration processes (the markers that dehydration
+ * releases) stay on the host.  *nchanged (may be NULL) = markers changed. */
+int des_phase_changes(des_ctx *ctx, int option, const int *hydrous_elemmarkers, int *nchanged);
+
+/* Download the device's marker material types ([nmarkers], may be NULL) and
+ * per-element marker counts ([nelem][nmat], may be NULL), for host-side
+ * marker bookkeeping before output, checkpoints or remeshing. */
+int des_get_markers(des_ctx *ctx, int *mattype, int *elemmarkers);
+
 /* Replace the parameters (e.g. after a change of max_vbc_val). */
 int des_set_params(des_ctx *ctx, const des_params *param);
 
@@ -258,6 +288,67 @@ int des_update_mesh(des_ctx *ctx);         /* dynearthsol.cxx:221-232 (surface_p
 /* Worst element quality and its index (geometry.cxx:458-512, used by
  * bad_mesh_quality, remeshing.cxx:1882-1935). */
 int des_worst_elem_quality(des_ctx *ctx, double *quality, int *elem);
+
+/* The mesh-quality check that triggers remeshing, bad_mesh_quality
+ * (remeshing.cxx:1882-1935), on the device-resident mesh: no coordinate or
+ * volume download.  It returns, in *code, the reference's value:
+ *   3  an element is smaller than smallest_size x the volume of the
+ *      equilateral tetrahedron (triangle) of side resolution; *index = the
+ *      first such element, *value = its volume;
+ *   2  (remeshing_option 1, 2 or 11) a bottom node (BOUNDZ0) lies farther
+ *      than max_boundary_distortion x resolution from z = -zlength;
+ *      *index = the first such node, *value = its z;
+ *   1  the worst element quality (elem_quality, geometry.cxx:458-496; its
+ *      cube root in 3D) is below min_quality; *index = the first worst
+ *      element, *value = that quality;
+ *   0  none of these; *index and *value are left unchanged.
+ * The checks run in that order, as the reference's do.  zlength is the
+ * context's des_params.zlength. */
+typedef struct des_quality_params {
+    double smallest_size;            /* Param::mesh.smallest_size */
+    double resolution;               /* Param::mesh.resolution */
+    double min_quality;              /* Param::mesh.min_quality */
+    double max_boundary_distortion;  /* Param::mesh.max_boundary_distortion */
+    int remeshing_option;            /* Param::mesh.remeshing_option */
+} des_quality_params;
+int des_bad_mesh_quality(des_ctx *ctx, const des_quality_params *qp, int *code, int *index, double *value);
+
+/* ---- the remesh hand-off ---------------------------------------------
+ * A mesh as remeshing leaves it (remeshing.cxx:1937-2035): connectivity,
+ * boundary flags and the boundary segments with their flags
+ * (Variables::segment, segflag), in the mesher's order. */
+typedef struct des_topology {
+    int ndims, nnode, nelem;
+    const int *connectivity;   /* [nelem][ndims+1] */
+    const unsigned *bcflag;    /* [nnode] */
+    int nseg;
+    const int *segment;        /* [nseg][ndims] node ids of each boundary segment */
+    const int *segflag;        /* [nseg] its boundary flag (0: not on a boundary) */
+} des_topology;
+
+/* create_support (mesh.cxx:1707-1721) and create_boundary_facets
+ * (mesh.cxx:1637-1704) built on the device (the reference's facet search is
+ * O(nseg x nelem); here one thread per segment searches the support list of
+ * one of its nodes), with the reference's results bit for bit: sup_off
+ * [nnode+1] and sup_elem [nelem*(ndims+1)], each node's elements in
+ * ascending order; bfacet_offsets [DES_NBDRYTYPES+1] and bfacets
+ * [nfacets][2] = (element, local facet), each boundary's facets in segment
+ * order.  Any output may be NULL.  Needs no context; work is queued on
+ * stream (NULL: the legacy default stream) and allocates temporary device
+ * memory.  A segment that matches no element facet is DES_EASSERT, as the
+ * reference exits with code 12. */
+int des_build_topology(const des_topology *topo, int *sup_off, int *sup_elem, int *bfacet_offsets,
+                       int *bfacets, void *stream);
+
+/* The device half of reallocate_variables (fields.cxx:51-93) and the
+ * topology rebuild after remeshing: the context's mesh becomes topo, its
+ * support lists and boundary facets built on the device, its device arrays
+ * sized for the new mesh.  Parameters, material table, boundary normals,
+ * precision and stream are kept; per-element overrides (des_set_elem_field)
+ * and device markers are dropped.  elemmarkers [nelem][nmat] are the new
+ * mesh's marker counts (required with nmat > 1).  The state is then
+ * uploaded with des_upload_state (the interpolated fields). */
+int des_remesh(des_ctx *ctx, const des_topology *topo, const int *elemmarkers);
 
 /* Read or set the context's dt / time / steps (Variables::dt, time, steps). */
 int des_get_clock(des_ctx *ctx, double *time, double *dt, int *steps);
@@ -387,10 +478,14 @@ int des_adjoint_backward(des_ctx *ctx, const des_host_state *seed, des_host_stat
  * allocating call.  All calls share that array and it keeps the last call's
  * contents (each call overwrites every entry it reads, so nothing needs
  * clearing); calls that overlap on the GPU (different streams, or different
- * host threads) race on it and must be serialised by the caller.  The first
- * call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture. */
+ * host threads) race on it and must be serialised by the caller.  Each call
+ * made outside stream capture looks up the array's device address
+ * (cudaGetSymbolAddress) on the current device, so a device reset between
+ * calls is harmless; a call inside a capture reuses the address of the last
+ * lookup on that device, so make the first call on each device before any
+ * stream capture, and none inside a capture after a device reset.  A CUDA
+ * error already pending on the calling thread is reported as DES_ECUDA
+ * without being cleared, and nothing is launched. */
 #define DES_NOALLOC_MAX_NODES 2097152
 int des_nmd_stress_noalloc(int ndims, int nnode, int nelem, const int *conn, const int *sup_off,
                            const int *sup_ent, const double *dpressure, const double *volume,

@@ -3,10 +3,12 @@
 * ``Oracle``: the C restatement in des_oracle.c (liboracle.so), runnable on
   any host; tests, the smoke check and bench.py's CPU-baseline leg use it as
   the checker.
-* ``Reference``: the reference's own hot-path sources compiled here by
-  ``make -C oracle ref`` (oracle/_ref/libref{2,3}d.so); only where the
-  reference tree exists.  Used to pin the restatement and to generate the
-  golden fixtures.
+* ``Reference``: the reference's own hot-path sources compiled by
+  ``make -C oracle ref`` (oracle/_ref/libref{2,3}d.so) from the staged copy
+  of its sources (oracle/_ref/src); only where those are staged.  Used to
+  pin the restatement, to generate the golden fixtures, as the CPU baseline
+  (the OpenMP build) and, linked with the device shim, to run the
+  reference's own loop body on the GPU.
 """
 from __future__ import annotations
 
@@ -33,12 +35,20 @@ def build_oracle(force: bool = False, perturbed: bool = False) -> str:
     return lib
 
 
-def build_reference() -> bool:
-    """Compile the reference sources (needs the reference tree)."""
-    ref = os.environ.get("DES_REFERENCE_DIR", "/root/reference")
-    if not os.path.isdir(ref):
+def reference_sources_available() -> bool:
+    """The reference's sources are staged under oracle/_ref/src, or the
+    reference tree is named by DES_REFERENCE_DIR (make -C oracle stage)."""
+    return bool(os.environ.get("DES_REFERENCE_DIR")) or os.path.isfile(os.path.join(REF_DIR, "src", "fields.cxx"))
+
+
+def build_reference(targets=("ref",)) -> bool:
+    """Compile the reference sources (make -C oracle ref), staging them first
+    from DES_REFERENCE_DIR when that is set; False when neither the staged
+    sources nor the tree are available."""
+    if not reference_sources_available():
         return False
-    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={ref}"])
+    ref = os.environ.get("DES_REFERENCE_DIR")
+    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, *targets] + ([f"REF={ref}"] if ref else []))
     return True
 
 
@@ -154,15 +164,55 @@ class RefIC(C.Structure):
         "xlength", "ylength", "zlength", "resolution")]
 
 
-class Reference:
-    """The reference's own functions (compiled from its sources)."""
+class RefQuality(C.Structure):
+    """The Param::mesh fields bad_mesh_quality reads (ref_quality in
+    oracle/ref_harness.cxx)."""
+    _fields_ = [(n, C.c_double) for n in ("smallest_size", "resolution", "min_quality",
+                                          "max_boundary_distortion", "zlength")] + [("remeshing_option", C.c_int)]
 
-    def __init__(self, ndims: int):
-        path = os.path.join(REF_DIR, f"libref{ndims}d.so")
+
+SHIM_BUILD = os.path.join(os.path.dirname(HERE), "dynearthsol_gb300", "shim", "_build")
+
+
+class Reference:
+    """The reference's own functions (compiled from its sources).
+
+    flavour "serial" is the 1-thread parity build (libref{2,3}d.so), "omp"
+    the OpenMP build (libref3d_omp.so, the CPU baseline), and "shim" the
+    reference harness and the reference's other objects linked with the
+    device shim in place of fields.o, geometry.o and rheology.o
+    (dynearthsol_gb300/shim: the reference's loop body on the GPU)."""
+
+    def __init__(self, ndims: int, flavour: str = "serial"):
+        if flavour == "serial":
+            path = os.path.join(REF_DIR, f"libref{ndims}d.so")
+        elif flavour == "omp":
+            path = os.path.join(REF_DIR, f"libref{ndims}d_omp.so")
+        elif flavour == "shim":
+            path = os.path.join(SHIM_BUILD, f"libref_shim{ndims}d.so")
+        else:
+            raise ValueError(flavour)
         if not os.path.exists(path):
-            raise OSError(f"{path} missing (make -C oracle ref)")
+            raise OSError(f"{path} missing (make -C oracle ref refomp; make -C dynearthsol_gb300/shim lib)")
         self.lib = C.CDLL(path)
         L = self.lib
+        L.ref_run_timed.argtypes = [C.POINTER(capi.DesMesh), C.POINTER(capi.DesParams),
+                                    C.POINTER(capi.DesMaterial), C.POINTER(capi.DesHostState), C.c_int,
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.ref_bad_mesh_quality.argtypes = [C.POINTER(capi.DesMesh), C.POINTER(capi.DesParams),
+                                           C.POINTER(capi.DesMaterial), C.POINTER(RefQuality),
+                                           C.POINTER(capi.DesHostState), C.POINTER(C.c_int)]
+        L.ref_nthreads.restype = C.c_int
+        L.ref_set_threads.argtypes = [C.c_int]
+        L.ref_create_support.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int)]
+        L.ref_create_boundary_facets.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_uint),
+                                                 C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.ref_phase_changes.argtypes = [C.POINTER(capi.DesMesh), C.POINTER(capi.DesParams),
+                                        C.POINTER(capi.DesMaterial), C.POINTER(capi.DesHostState), C.c_int,
+                                        C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.ref_init.argtypes = [C.POINTER(capi.DesMesh), C.POINTER(capi.DesParams),
                                C.POINTER(capi.DesMaterial), C.POINTER(RefIC),
                                C.POINTER(capi.DesHostState), C.POINTER(C.c_double),
@@ -199,6 +249,67 @@ class Reference:
         self.lib.ref_run(C.byref(cs.mesh), C.byref(cs.params), C.byref(cs.mat), C.byref(hs),
                          nsteps, capi.dptr(dts))
         return (hs.time, hs.dt, hs.steps), dts[:nsteps]
+
+    def run_timed(self, wl: Workload, st: dict, comp: float, clock, nsteps: int):
+        """nsteps of the loop body; returns (clock, wall seconds of the loop alone)."""
+        cs = CStructs(wl, comp)
+        hs = capi.host_state_struct(st, *clock)
+        sec = C.c_double()
+        self.lib.ref_run_timed(C.byref(cs.mesh), C.byref(cs.params), C.byref(cs.mat), C.byref(hs),
+                               nsteps, None, C.byref(sec))
+        return (hs.time, hs.dt, hs.steps), sec.value
+
+    def nthreads(self) -> int:
+        return self.lib.ref_nthreads()
+
+    def set_threads(self, n: int):
+        """OpenMP threads of the following calls (the OpenMP build)."""
+        self.lib.ref_set_threads(n)
+
+    def bad_mesh_quality(self, wl: Workload, st: dict, comp: float, clock, rq: RefQuality):
+        """bad_mesh_quality (remeshing.cxx:1882-1935): (code, index)."""
+        cs = CStructs(wl, comp)
+        hs = capi.host_state_struct(st, *clock)
+        idx = C.c_int(-1)
+        code = self.lib.ref_bad_mesh_quality(C.byref(cs.mesh), C.byref(cs.params), C.byref(cs.mat),
+                                             C.byref(rq), C.byref(hs), C.byref(idx))
+        return code, idx.value
+
+    def create_support(self, nnode: int, conn: np.ndarray):
+        """create_support (mesh.cxx:1707-1721) as CSR (off[nnode+1], elems)."""
+        conn = np.ascontiguousarray(conn, dtype=np.int32)
+        off = np.zeros(nnode + 1, np.int32)
+        elems = np.zeros(conn.size, np.int32)
+        self.lib.ref_create_support(nnode, conn.shape[0], capi.iptr(conn), capi.iptr(off), capi.iptr(elems))
+        return off, elems
+
+    def create_boundary_facets(self, nnode: int, conn, bcflag, segment, segflag):
+        """create_boundary_facets (mesh.cxx:1637-1704): (offsets[11], facets[n][2])."""
+        conn = np.ascontiguousarray(conn, dtype=np.int32)
+        bcflag = np.ascontiguousarray(bcflag, dtype=np.uint32)
+        segment = np.ascontiguousarray(segment, dtype=np.int32)
+        segflag = np.ascontiguousarray(segflag, dtype=np.int32)
+        off = np.zeros(capi.NBDRY + 1, np.int32)
+        fac = np.zeros((segment.shape[0], 2), np.int32)
+        self.lib.ref_create_boundary_facets(nnode, conn.shape[0], capi.iptr(conn), capi.uptr(bcflag),
+                                            segment.shape[0], capi.iptr(segment), capi.iptr(segflag),
+                                            capi.iptr(off), capi.iptr(fac))
+        return off, fac[:off[-1]]
+
+    def phase_changes(self, wl: Workload, st: dict, comp: float, option: int, elem, eta, mattype, hydem,
+                      elemmarkers):
+        """phase_changes (phasechanges.cxx:232-258): (new material types, new marker counts)."""
+        cs = CStructs(wl, comp)
+        hs = capi.host_state_struct(st)
+        elem = np.ascontiguousarray(elem, dtype=np.int32)
+        eta = np.ascontiguousarray(eta, dtype=np.float64)
+        mt = np.array(mattype, dtype=np.int32)
+        hyd = None if hydem is None else np.ascontiguousarray(hydem, dtype=np.int32)
+        em = np.array(elemmarkers, dtype=np.int32)
+        self.lib.ref_phase_changes(C.byref(cs.mesh), C.byref(cs.params), C.byref(cs.mat), C.byref(hs), option,
+                                   elem.shape[0], capi.iptr(elem), capi.dptr(eta), capi.iptr(mt), capi.iptr(hyd),
+                                   capi.iptr(em))
+        return mt, em
 
     def call(self, wl: Workload, st: dict, comp: float, clock, name: str):
         cs = CStructs(wl, comp)

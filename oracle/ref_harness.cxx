@@ -11,8 +11,13 @@
  * (dynearthsol.cxx:82-98) and the loop body (dynearthsol.cxx:325-361,
  * without phase changes, output and remeshing), and copies the fields back.
  */
+#include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
+#ifdef USE_OMP
+#include <omp.h>
+#endif
 
 #include "constants.hpp"
 #include "parameters.hpp"
@@ -23,6 +28,10 @@
 #include "bc.hpp"
 #include "ic.hpp"
 #include "binaryio.hpp"
+#include "remeshing.hpp"
+#include "mesh.hpp"
+#include "markerset.hpp"
+#include "phasechanges.hpp"
 
 #include "../include/desgpu.h"
 
@@ -31,7 +40,49 @@
  * option, so a stub satisfies the linker. */
 void read_external_temperature_from_comsol(const Param &, const Variables &, double_vec &) {}
 
+#ifndef THREED
+/* The 2D mesh.cxx keeps a reference to Triangle's entry points after the
+ * unused meshing code is dropped; the harness never meshes, so stubs that
+ * stop the program satisfy the linker. */
+struct triangulateio;
+void triangulate(char *, triangulateio *, triangulateio *, triangulateio *) { std::abort(); }
+void trifree(void *) { std::abort(); }
+#endif
+
+/* Hooks of a device shim linked in place of fields.o, geometry.o and
+ * rheology.o (a library that keeps Variables on a device between calls):
+ * the host program uploads Variables after changing them and downloads them
+ * before reading them.  Weak, so that they are null in the plain reference
+ * build. */
+extern "C" void desgpu_shim_sync_to_host(void) __attribute__((weak));
+extern "C" void desgpu_shim_sync_to_device(void) __attribute__((weak));
+
 extern "C" {
+
+/* The Param::mesh fields bad_mesh_quality reads (parameters.hpp:52-80). */
+typedef struct ref_quality {
+    double smallest_size, resolution, min_quality, max_boundary_distortion, zlength;
+    int remeshing_option;
+} ref_quality;
+
+int ref_nthreads(void)
+{
+#ifdef USE_OMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* OpenMP threads of the following calls (the element bands follow them) */
+void ref_set_threads(int n)
+{
+#ifdef USE_OMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
 
 typedef struct ref_ic {
     int weakzone_option;
@@ -180,7 +231,19 @@ void build_model(Model &md, const des_mesh *mesh, const des_params *dp, const de
             var.bfacets[i].push_back(std::make_pair(mesh->bfacets[2 * q], mesh->bfacets[2 * q + 1]));
     var.support = NULL;
     var.egroups.clear();
+#ifdef USE_OMP
+    /* the element bands of the OpenMP build: 2T contiguous bands of equal
+     * size, the last one taking the remainder, as create_elem_groups lays
+     * them out (mesh.cxx:1724-1747); mesh.cxx itself needs TetGen and
+     * Triangle, so the harness forms the bands */
+    {
+        const int ngroups = 2 * omp_get_max_threads();
+        const int per = var.nelem / ngroups;
+        for (int i = 0; i < ngroups; ++i) var.egroups.push_back(i * per);
+    }
+#else
     var.egroups.push_back(0);
+#endif
     var.egroups.push_back(var.nelem);
     var.elemmarkers = new int_vec2D(var.nelem, std::vector<int>(dm->nmat, 0));
     for (int e = 0; e < var.nelem; ++e)
@@ -328,15 +391,19 @@ int ref_init(const des_mesh *mesh, const des_params *dp, const des_material *dm,
 }
 
 /* nsteps of the loop body (dynearthsol.cxx:325-361) on a given state.  When
- * record is not NULL, the (per-step) dt values are written there. */
-int ref_run(const des_mesh *mesh, const des_params *dp, const des_material *dm, des_host_state *st,
-            int nsteps, double *record_dt)
+ * record is not NULL, the (per-step) dt values are written there; when
+ * seconds is not NULL, the wall time of the loop alone (no model set-up or
+ * state copies). */
+int ref_run_timed(const des_mesh *mesh, const des_params *dp, const des_material *dm, des_host_state *st,
+                  int nsteps, double *record_dt, double *seconds)
 {
     Model md;
     build_model(md, mesh, dp, dm, NULL, st->coord);
     Variables &var = md.var;
     const Param &param = md.param;
     state_in(var, st);
+    if (desgpu_shim_sync_to_device) desgpu_shim_sync_to_device();
+    const auto t0 = std::chrono::steady_clock::now();
     for (int it = 0; it < nsteps; ++it) {
         var.steps++;
         var.time += var.dt;
@@ -357,8 +424,40 @@ int ref_run(const des_mesh *mesh, const des_params *dp, const des_material *dm, 
         if (var.steps % 10 == 0) var.dt = compute_dt(param, var);
         if (record_dt) record_dt[it] = var.dt;
     }
+    if (desgpu_shim_sync_to_host) desgpu_shim_sync_to_host();
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     state_out(var, st);
     return 0;
+}
+
+int ref_run(const des_mesh *mesh, const des_params *dp, const des_material *dm, des_host_state *st,
+            int nsteps, double *record_dt)
+{
+    return ref_run_timed(mesh, dp, dm, st, nsteps, record_dt, NULL);
+}
+
+/* The reference's bad_mesh_quality (remeshing.cxx:1882-1935) on a given
+ * state: returns its code (0 good, 1 element quality, 2 bottom node drift,
+ * 3 tiny element) and writes the index it reports. */
+int ref_bad_mesh_quality(const des_mesh *mesh, const des_params *dp, const des_material *dm,
+                         const ref_quality *rq, des_host_state *st, int *index)
+{
+    Model md;
+    build_model(md, mesh, dp, dm, NULL, st->coord);
+    Variables &var = md.var;
+    Param &param = md.param;
+    state_in(var, st);
+    param.mesh.smallest_size = rq->smallest_size;
+    param.mesh.resolution = rq->resolution;
+    param.mesh.min_quality = rq->min_quality;
+    param.mesh.max_boundary_distortion = rq->max_boundary_distortion;
+    param.mesh.zlength = rq->zlength;
+    param.mesh.remeshing_option = rq->remeshing_option;
+    if (desgpu_shim_sync_to_device) desgpu_shim_sync_to_device();
+    int idx = -1;
+    int code = bad_mesh_quality(param, var, idx);
+    *index = idx;
+    return code;
 }
 
 /* One reference function on a given state, by name; used to pin the
@@ -399,6 +498,101 @@ int ref_call(const des_mesh *mesh, const des_params *dp, const des_material *dm,
         result[1] = worst;
     } else return 1;
     state_out(var, st);
+    return 0;
+}
+
+/* The reference's create_support (mesh.cxx:1707-1721) of a connectivity,
+ * as CSR: off[nnode+1], elems[nelem*NODES_PER_ELEM]. */
+int ref_create_support(int nnode, int nelem, const int *conn, int *off, int *elems)
+{
+    Variables var = Variables();
+    var.nnode = nnode;
+    var.nelem = nelem;
+    var.connectivity = new conn_t(nelem);
+    std::memcpy(var.connectivity->data(), conn, sizeof(int) * NODES_PER_ELEM * nelem);
+    create_support(var);
+    off[0] = 0;
+    for (int n = 0; n < nnode; ++n) {
+        const int_vec &s = (*var.support)[n];
+        for (std::size_t k = 0; k < s.size(); ++k) elems[off[n] + k] = s[k];
+        off[n + 1] = off[n] + (int)s.size();
+    }
+    delete var.support;
+    delete var.connectivity;
+    return 0;
+}
+
+/* The reference's create_boundary_facets (mesh.cxx:1637-1704) of a mesh and
+ * its boundary segments (Variables::segment, segflag, as the mesher gives
+ * them): offsets[nbdrytypes+1], facets[nfacets][2] = (element, facet). */
+int ref_create_boundary_facets(int nnode, int nelem, const int *conn, const unsigned *bcflag, int nseg,
+                               const int *segment, const int *segflag, int *offsets, int *facets)
+{
+    Variables var = Variables();
+    var.nnode = nnode;
+    var.nelem = nelem;
+    var.nseg = nseg;
+    var.connectivity = new conn_t(nelem);
+    std::memcpy(var.connectivity->data(), conn, sizeof(int) * NODES_PER_ELEM * nelem);
+    var.bcflag = new uint_vec(bcflag, bcflag + nnode);
+    var.segment = new segment_t(nseg);
+    std::memcpy(var.segment->data(), segment, sizeof(int) * NDIMS * nseg);
+    var.segflag = new segflag_t(nseg);
+    std::memcpy(var.segflag->data(), segflag, sizeof(int) * nseg);
+    create_boundary_facets(var);
+    offsets[0] = 0;
+    for (int i = 0; i < nbdrytypes; ++i) {
+        for (std::size_t k = 0; k < var.bfacets[i].size(); ++k) {
+            facets[2 * (offsets[i] + k)] = var.bfacets[i][k].first;
+            facets[2 * (offsets[i] + k) + 1] = var.bfacets[i][k].second;
+        }
+        offsets[i + 1] = offsets[i] + (int)var.bfacets[i].size();
+    }
+    delete var.connectivity;
+    delete var.bcflag;
+    delete var.segment;
+    delete var.segflag;
+    return 0;
+}
+
+/* The reference's phase_changes (phasechanges.cxx:232-258), option
+ * phase_change_option, on a marker set given as arrays (element, barycentric
+ * eta[NODES_PER_ELEM], material type) and a state; hydem[nelem] are the
+ * hydrous-marker counts that SimpleSubduction reads.  Hydration processes
+ * are off.  Writes the new material types and marker counts
+ * (elemmarkers[nelem][nmat], in/out). */
+int ref_phase_changes(const des_mesh *mesh, const des_params *dp, const des_material *dm, des_host_state *st,
+                      int option, int nmarkers, const int *melem, const double *meta, int *mattype,
+                      const int *hydem, int *elemmarkers)
+{
+    Model md;
+    build_model(md, mesh, dp, dm, NULL, st->coord);
+    Variables &var = md.var;
+    Param &param = md.param;
+    state_in(var, st);
+    param.mat.phase_change_option = option;
+    param.control.has_hydration_processes = false;
+    const int nm = dm->nmat;
+    for (int e = 0; e < var.nelem; ++e)
+        for (int k = 0; k < nm; ++k) (*var.elemmarkers)[e][k] = elemmarkers[(size_t)e * nm + k];
+    MarkerSet *ms = new MarkerSet("markerset");
+    for (int m = 0; m < nmarkers; ++m) ms->append_marker(meta + (size_t)m * NODES_PER_ELEM, melem[m], mattype[m]);
+    MarkerSet *hyd = new MarkerSet("hydrous-markerset");
+    var.markersets.push_back(ms);
+    var.markersets.push_back(hyd);
+    var.hydrous_marker_index = 1;
+    var.hydrous_elemmarkers = new Array2D<int, 1>(var.nelem);
+    for (int e = 0; e < var.nelem; ++e) (*var.hydrous_elemmarkers)[e][0] = hydem ? hydem[e] : 0;
+    var.phch = NULL;
+    phase_changes_init(param, var);
+    phase_changes(param, var);
+    for (int m = 0; m < nmarkers; ++m) mattype[m] = ms->get_mattype(m);
+    for (int e = 0; e < var.nelem; ++e)
+        for (int k = 0; k < nm; ++k) elemmarkers[(size_t)e * nm + k] = (*var.elemmarkers)[e][k];
+    delete var.phch;
+    delete var.hydrous_elemmarkers;
+    delete hyd;
+    delete ms;
     return 0;
 }
 

@@ -5,7 +5,10 @@ set chosen to exercise one part of the hot path (plasticity in 2D/3D, plane
 strain, Maxwell/viscous/elastic rheologies, heat with radiogenic source,
 multi-material blending, per-element parameters, every velocity-BC family,
 damping options, jittered/permuted meshes).  Sizes are small enough for the
-reference and the oracle to run them in well under a second.
+reference and the oracle to run them in well under a second, except the
+full-horizon cases (FULL_CASES: the 2D workload at its full size over its
+10,000 steps, and a yielding case of the 3D workload's physics over its
+2000 steps), which take tens of seconds.
 """
 from __future__ import annotations
 
@@ -158,18 +161,70 @@ def build_case(name: str) -> tuple[Workload, int]:
             capi.EF_THERM_COND: np.ascontiguousarray(3.0 + rng.uniform(-0.5, 0.5, ne)),
         }
         return wl, n
+    if name == "2d_c0_full":
+        # the 2D workload at its full size and horizon: 200x20 cells x 2
+        # triangles (8,000 / 4,221 nodes), 10,000 steps, default damping
+        return make_workload("c0_2d_ep"), 10000
+    if name == "2d_c0_full_damp2":
+        wl, n = build_case("2d_c0_full")
+        wl.params = replace(wl.params, damping_option=2)
+        return wl, n
+    if name == "3d_c1_yield_band":
+        # the 3D workload's physics and boundary speeds on 20x20x6 cubes
+        # (14,400 tets) for the workload's 2000 steps, with a band of weak
+        # material that yields (9 % of the elements by the end)
+        wl = make_workload("c1_3d_evp", cells=(20, 20, 6))
+        return weak_band(wl), 2000
+    if name == "3d_c1_yield_band_damp2":
+        wl, n = build_case("3d_c1_yield_band")
+        wl.params = replace(wl.params, damping_option=2)
+        return wl, n
     raise KeyError(name)
+
+
+def weak_band(wl: Workload, halfwidth: float = 15e3, cohesion=(1e6, 1e5), friction=(10.0, 5.0)) -> Workload:
+    """Two materials: the workload's own outside the vertical band
+    |x - xlength/2| < halfwidth (element centroids), and inside it the same
+    material with low cohesion (cohesion0/1) and friction (friction_angle0/1),
+    one marker per element (a marker-blended multi-material mesh,
+    matprops.cxx:103-128).  At the workload's boundary speeds the band
+    reaches the Mohr-Coulomb yield surface within a few hundred steps."""
+    from dynearthsol_gb300.config import elem_center
+    mt = wl.mat
+    two = {n: tuple(getattr(mt, n)) * 2 for n in capi.MAT_ARRAYS}
+    two["cohesion0"] = (mt.cohesion0[0], cohesion[0])
+    two["cohesion1"] = (mt.cohesion1[0], cohesion[1])
+    two["friction_angle0"] = (mt.friction_angle0[0], friction[0])
+    two["friction_angle1"] = (mt.friction_angle1[0], friction[1])
+    band = np.abs(elem_center(wl.mesh)[:, 0] - 0.5 * wl.mesh.lengths[0]) < halfwidth
+    em = np.zeros((wl.mesh.nelem, 2), np.int32)
+    em[~band, 0] = 1
+    em[band, 1] = 1
+    wl.mat = replace(mt, elemmarkers=em, **two)
+    return wl
 
 
 CASES = ["2d_ep", "2d_ep_yield", "2d_evp_heat", "2d_ps_oedometer", "3d_evp", "3d_evp_yield",
          "3d_ep_yield", "3d_maxwell", "3d_elastic_damp3", "3d_viscous", "3d_heat_jitter_multimat",
          "3d_vbc_mix", "3d_slant_n0_t1", "3d_slant_n0_t11", "3d_slant_n0_t13", "2d_slant_n0_t3",
-         "3d_percell"]
+         "3d_percell"] + ["2d_c0_full", "2d_c0_full_damp2", "3d_c1_yield_band", "3d_c1_yield_band_damp2"]
+
+# the full-horizon cases: the 2D workload at full size over 10,000 steps and
+# a yielding case of the 3D workload's physics over 2000 steps, each with a
+# damping-option-2 twin (no copysign damping: not chaotic, see the tests)
+FULL_CASES = ["2d_c0_full", "2d_c0_full_damp2", "3d_c1_yield_band", "3d_c1_yield_band_damp2"]
 
 # cases whose fixture also holds a mid-run state and the output of every
 # reference function applied to it
-PERFN_CASES = ["2d_evp_heat", "3d_heat_jitter_multimat", "3d_evp_yield", "2d_ps_oedometer"]
+PERFN_CASES = ["2d_evp_heat", "3d_heat_jitter_multimat", "3d_evp_yield", "2d_ps_oedometer",
+               "3d_c1_yield_band_damp2"]
 PERFN_MID_STEPS = 60
+# the yielding band's mid-run state comes later, once 7 % of its elements yield
+MID_STEPS = {"3d_c1_yield_band_damp2": 1500}
+
+
+def mid_steps(name: str) -> int:
+    return MID_STEPS.get(name, PERFN_MID_STEPS)
 
 FUNCTIONS = {
     "update_temperature": ["temperature", "ntmp"],

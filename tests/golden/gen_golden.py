@@ -10,11 +10,13 @@ every case of tests/cases.py it stores, bit for bit:
   normals, velocity BCs, initial stress, weak zone, dt);
 * ``final/*`` -- the state after ``nsteps`` of the loop body
   (dynearthsol.cxx:325-361) and the dt of every step;
-* for the per-function cases, ``mid/*`` (the state after 60 steps),
+* for the per-function cases, ``mid/*`` (the state after 60 steps, or
+  ``cases.MID_STEPS``),
   ``fn_<name>/*`` -- the fields each reference function writes when applied
   once to ``mid`` (plus compute_dt and worst_elem_quality results) -- and
   ``mid1/*``, ``mid10/*``: the state 1 and 10 steps after ``mid``, with
   their envelopes ``envelope_mid1/*``, ``envelope_mid10/*`` (below);
+  the full-horizon cases keep fewer fields (``kept``) and no ``fn_*``;
 * ``envelope/<field>`` -- the libm sensitivity of the case: the largest
   normalised deviation from ``final`` of three runs of the restatement whose
   transcendental results are moved by +-1 ulp (seeds 1, 2, 3).  Any faithful
@@ -37,11 +39,23 @@ sys.path.insert(0, os.path.dirname(HERE))
 
 from dataclasses import replace  # noqa: E402
 
-from cases import CASES, FUNCTIONS, PERFN_CASES, PERFN_MID_STEPS, build_case, reference_material_for  # noqa: E402
+from cases import (CASES, FULL_CASES, FUNCTIONS, PERFN_CASES, build_case, mid_steps,  # noqa: E402
+                   reference_material_for)
 from dynearthsol_gb300.config import initial_state  # noqa: E402
 from oracle.oracle import Oracle, Reference, build_reference, state_copy  # noqa: E402
 
-ENVELOPE_FIELDS = ("vel", "stress", "temperature", "plstrain", "coord", "strain", "force")
+ENVELOPE_FIELDS = ("vel", "stress", "temperature", "plstrain", "coord", "strain", "force", "delta_plstrain")
+# the full-horizon cases are large (up to 14,400 tets): their final and
+# mid+k states keep the compared fields only (fewer in 3D), and they keep no
+# per-function outputs (the one-step run from mid checks every function)
+LEAN_FIELDS_2D = ENVELOPE_FIELDS + ("volume", "dpressure", "delta_plstrain")
+LEAN_FIELDS_3D = ("vel", "stress", "temperature", "plstrain", "coord", "delta_plstrain")
+
+
+def kept(name: str, k: str) -> bool:
+    if name not in FULL_CASES:
+        return True
+    return k in (LEAN_FIELDS_2D if name.startswith("2d") else LEAN_FIELDS_3D)
 
 
 def envelope(wl, start, cp, clk, nsteps, result):
@@ -75,11 +89,13 @@ def gen(name: str) -> str:
     out["init/compensation_pressure"] = np.array(cp)
     if name in PERFN_CASES:
         mid = state_copy(st)
-        clk_mid, _ = ref.run(wl_ref, mid, cp, clk, PERFN_MID_STEPS)
+        clk_mid, _ = ref.run(wl_ref, mid, cp, clk, mid_steps(name))
         for k, v in mid.items():
             out[f"mid/{k}"] = v.copy()
         out["mid/clock"] = np.array(clk_mid, dtype=np.float64)
         for fn, fields in FUNCTIONS.items():
+            if name in FULL_CASES:
+                continue
             s = state_copy(mid)
             ref.call(wl_ref, s, cp, clk_mid, fn)
             for f in fields:
@@ -88,7 +104,8 @@ def gen(name: str) -> str:
             s = state_copy(mid)
             clk_k, _ = ref.run(wl_ref, s, cp, clk_mid, k_steps)
             for k, v in s.items():
-                out[f"mid{k_steps}/{k}"] = v.copy()
+                if kept(name, k):
+                    out[f"mid{k_steps}/{k}"] = v.copy()
             out[f"mid{k_steps}/clock"] = np.array(clk_k, dtype=np.float64)
             for f, v in envelope(wl, mid, cp, clk_mid, k_steps, s).items():
                 out[f"envelope_mid{k_steps}/{f}"] = np.array(v)
@@ -101,7 +118,8 @@ def gen(name: str) -> str:
     init_state = state_copy(st)
     clk_f, dts = ref.run(wl_ref, st, cp, clk, nsteps)
     for k, v in st.items():
-        out[f"final/{k}"] = v.copy()
+        if kept(name, k):
+            out[f"final/{k}"] = v.copy()
     for f, v in envelope(wl, init_state, cp, clk, nsteps, st).items():
         out[f"envelope/{f}"] = np.array(v)
     out["final/clock"] = np.array(clk_f, dtype=np.float64)

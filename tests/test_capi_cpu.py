@@ -8,7 +8,6 @@ import pytest
 from dynearthsol_gb300 import capi
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("DES_REFERENCE_DIR", "/root/reference")
 
 
 @pytest.fixture(scope="module")
@@ -73,14 +72,21 @@ def _defined_functions(obj):
     return names
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+def _reference_sources():
+    from oracle.oracle import reference_sources_available
+    return reference_sources_available()
+
+
+@pytest.mark.skipif(not _reference_sources(), reason="reference sources not staged (make -C oracle stage REF=...)")
 @pytest.mark.parametrize("nd", [2, 3])
 def test_shim_replaces_fields_geometry_rheology(lib, nd):
     """The shim links in place of the reference's fields.o, geometry.o and
     rheology.o: it defines every function they define (same C++ signatures)
     and links with the rest of the reference with no undefined symbol."""
+    from oracle.oracle import build_reference
+    assert build_reference()
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "dynearthsol_gb300", "shim"),
-                           f"ND={nd}", f"REF={REF}", "linkcheck"])
+                           f"ND={nd}", "lib"])
     build = os.path.join(ROOT, "dynearthsol_gb300", "shim", "_build")
     shim = _defined_functions(os.path.join(build, f"des_shim{nd}d.o"))
     refobj = os.path.join(ROOT, "oracle", "_ref", f"obj{nd}d")

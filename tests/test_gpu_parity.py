@@ -113,6 +113,8 @@ def test_gpu_steps_from_mid_state(name, k_steps, tol):
 @pytest.mark.parametrize("fn", list(FUNCTIONS))
 def test_gpu_functions_match_reference(name, fn):
     g = load_golden(name)
+    if f"fn_{fn}" not in g:
+        pytest.skip(f"{name} keeps no {fn} output (full-horizon fixture)")
     wl, _ = build_case(name)
     m = _model(wl, float(g["init"]["compensation_pressure"]))
     c = g["mid"]["clock"]

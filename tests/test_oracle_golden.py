@@ -71,6 +71,8 @@ def test_oracle_run_matches_reference(name):
 @pytest.mark.parametrize("fn", list(FUNCTIONS))
 def test_oracle_functions_match_reference(name, fn):
     g = load_golden(name)
+    if f"fn_{fn}" not in g:
+        pytest.skip(f"{name} keeps no {fn} output (full-horizon fixture)")
     wl, _ = build_case(name)
     st = state_from(g["mid"])
     clk = tuple(g["mid"]["clock"])
