@@ -384,6 +384,8 @@ def main():
                          "its forward, or every 50 steps when that tape does not fit in device memory)")
     ap.add_argument("--adjoint-fd", type=int, default=20,
                     help="elements checked against central differences in the adjoint benchmark")
+    ap.add_argument("--yield-spinup", type=int, default=8000,
+                    help="mixed steps that bring the weak band of the yielding benchmark to yield (0: skip it)")
     ap.add_argument("--yield-adjoint-steps", type=int, default=100,
                     help="window of the adjoint with yielding elements (cohesion and friction gradients; 0: skip)")
     ap.add_argument("--heat-adjoint-steps", type=int, default=200,
@@ -484,6 +486,9 @@ def main():
     adjoint = None
     if args.adjoint_steps > 0 and rank == 0:
         adjoint = adjoint_bench(args, stream)
+    yielding = None
+    if args.yield_spinup > 0 and rank == 0:
+        yielding = yield_bench(args, stream)
     yield_adjoint = None
     if args.yield_adjoint_steps > 0 and rank == 0:
         yield_adjoint = yield_adjoint_bench(args, stream)
@@ -507,6 +512,7 @@ def main():
             "mixed_vs_fp64": compare,
             "mixed_error_gate": gate,
             "e2e": e2e,
+            "yield": yielding,
             "adjoint": adjoint,
             "yield_adjoint": yield_adjoint,
             "heat_adjoint": heat_adjoint,
@@ -723,6 +729,59 @@ def yield_adjoint_bench(args, stream):
             "fd_check": checks, "fd_max_rel_err": max((r["rel_err"] for r in checks), default=None),
             "fd_cohesion1_direction": {"adjoint": gn, "central_fd": float(dfd),
                                        "rel_err": float(abs(dfd - gn) / max(abs(dfd), gn))}}
+
+
+def yield_bench(args, stream):
+    """Both steps where the Mohr-Coulomb return map is active: the 3D
+    workload's mesh (998,400 tets) with a 30 km band of weak material
+    (cohesion 1 -> 0.1 MPa, friction 10 -> 5 degrees), spun up with the
+    mixed step until the band yields, then args.steps timed steps of each
+    precision from that state.  Reports the throughputs, the elements that
+    yield in the window and in its last step, and the mixed step's stress
+    error against the FP64 run from the same state (reported, not gated:
+    the yielding reference is itself chaotic under one-ulp changes)."""
+    import torch
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import initial_state, make_workload, weak_band
+    from dynearthsol_gb300.solver import DeviceModel
+    wl = weak_band(make_workload("c1_3d_evp"))
+    st, cp = initial_state(wl)
+    m = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_MIXED, stream=stream.cuda_stream)
+    init = m.init_fields(st)
+    m.step(args.yield_spinup)
+    start = m.download()
+    clock = m.clock()
+    ne = wl.mesh.nelem
+    out = {"workload": "c1_3d_evp mesh with a weak band (2 materials)", "nelem": ne,
+           "spinup_steps": args.yield_spinup, "window_steps": args.steps}
+    res = {}
+    for name, prec in (("fp64", capi.PREC_FP64), ("mixed", capi.PREC_MIXED)):
+        d = m if prec == capi.PREC_MIXED else DeviceModel(wl, comp_pressure=cp, precision=prec,
+                                                          stream=stream.cuda_stream)
+        d.upload({k: v.copy() for k, v in start.items()}, clock)
+        d.step(args.warmup)
+        d.upload({k: v.copy() for k, v in start.items()}, clock)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        d.step(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        fin = d.download()
+        res[name] = fin
+        out[name] = {"value": ne * args.steps / (ms / 1e3) / 1e6, "unit": "Mtet-steps/s",
+                     "ms_per_step": ms / args.steps,
+                     "yielded_in_window": int((fin["plstrain"] > start["plstrain"] + 1e-12).sum()),
+                     "yielding_last_step": int((fin["delta_plstrain"] > 0).sum())}
+        if d is not m:
+            d.close()
+    a, b = res["fp64"], res["mixed"]
+    out["speedup_mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["mixed_vs_fp64_stress_rel_l2"] = float(np.linalg.norm(b["stress"] - a["stress"]) / np.linalg.norm(a["stress"]))
+    out["yielded_at_start"] = int((start["plstrain"] > init["plstrain"] + 1e-12).sum())
+    m.close()
+    return out
 
 
 def scale_bench(args, stream):

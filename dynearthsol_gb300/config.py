@@ -400,3 +400,22 @@ def make_workload(name: str, scale: float = 1.0, seed: int = 12345, cells: tuple
     raise KeyError(name)
 
 
+def weak_band(wl: Workload, halfwidth: float = 15e3, cohesion=(1e6, 1e5), friction=(10.0, 5.0)) -> Workload:
+    """Two materials: the workload's own outside the vertical band
+    |x - xlength/2| < halfwidth (element centroids), and inside it the same
+    material with low cohesion (cohesion0/1) and friction (friction_angle0/1),
+    one marker per element (a marker-blended multi-material mesh,
+    matprops.cxx:103-128).  At the workload's boundary speeds the band
+    reaches the Mohr-Coulomb yield surface within a few hundred steps."""
+    mt = wl.mat
+    two = {n: tuple(getattr(mt, n)) * 2 for n in capi.MAT_ARRAYS}
+    two["cohesion0"] = (mt.cohesion0[0], cohesion[0])
+    two["cohesion1"] = (mt.cohesion1[0], cohesion[1])
+    two["friction_angle0"] = (mt.friction_angle0[0], friction[0])
+    two["friction_angle1"] = (mt.friction_angle1[0], friction[1])
+    band = np.abs(elem_center(wl.mesh)[:, 0] - 0.5 * wl.mesh.lengths[0]) < halfwidth
+    em = np.zeros((wl.mesh.nelem, 2), np.int32)
+    em[~band, 0] = 1
+    em[band, 1] = 1
+    wl.mat = replace(mt, elemmarkers=em, **two)
+    return wl

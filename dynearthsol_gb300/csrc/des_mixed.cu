@@ -135,6 +135,104 @@ __device__ __forceinline__ void elastic_mixed(double bulkm, double shearm, const
     for (int i = 3; i < 6; ++i) s[i] = fma(g2, de[i], s[i]);
 }
 
+// ------------------------------------------------------------------
+// The mixed EVP branch in increment form.  Both candidates of the branch
+// choice (rheology.cxx:594-634) are the old stress s plus an FP32 increment
+// added in FP64:
+//   Maxwell (rheology.cxx:118-134)  dv = c1 x + f2 y + K dv_vol   (normal),
+//                                        c1 x + f2 y              (shear),
+//   elastic trial (elastic_)        dp = y + K tr(de)             (normal),
+//                                        y                        (shear),
+// x the old deviator (s_i - s0 for the normal components, the old shear
+// stress), y = 2G (de - tr(de)/3) (normal) and 2G de (shear) the trial's
+// deviatoric increment, f2 = 1 / (1 + tmp), c1 = f1 f2 - 1 = -2 tmp f2
+// with f1 = 1 - tmp and tmp = dt G / (2 visc): the Maxwell update
+// (x f1 + y) f2 + s0 + K dv_vol less the old stress.  The increments are
+// small against the stress (a few hundred Pa per step against ~1e8 Pa in
+// the 998,400-tet workload), so their FP32 rounding (~2^-23 of themselves)
+// moves the stress by ~1e-5 Pa per step, while the FP64 additions keep the
+// state's own precision: 6 FP64 additions per candidate instead of the 16
+// FP64 operations of the FP64-coefficient update.
+// ------------------------------------------------------------------
+struct MaxwellF {
+    float c1, f2;
+};
+
+__device__ __forceinline__ MaxwellF maxwell_coef_f(double shearm, double viscosity, double dt)
+{
+    const float tf = (0.5f * f32_of(dt) * f32_of(shearm)) / f32_of(viscosity);
+    const float f2 = 1.0f / (1.0f + tf);
+    return {-2.0f * tf * f2, f2};
+}
+
+// relative volume change vol / vol_old - 1 in FP32 from the FP64 difference
+// (exact for volumes within a factor 2 of each other)
+__device__ __forceinline__ float dvol_f(const KP &p, int e)
+{
+    const double vo = p.vol_old[e];
+    return f32_of(p.vol[e] - vo) / f32_of(vo);
+}
+
+// The branch choice svII < spII of the mixed step, decided from FP32 values
+// where an identity allows.  The comparison it stands for is the FP64 one of
+// the FP64 candidates (those the branch forms where the screen is
+// undecided): the elastic trial sp = elastic_mixed(s, de) and the Maxwell
+// update sv = maxwell_mixed_xy(x, y) with f1 = 1 - tmp, f2 = 1 / (1 + tmp).
+// Their exact deviators are q = x + y and f2 (q - tmp x), so
+//   J2(sv) - J2(sp) = -f2^2 tmp Q,  Q = (2 + tmp) J(q) + 2 <q, x> - tmp J(x),
+// J(v) = (v0^2 + v1^2 + v2^2) / 2 + v3^2 + v4^2 + v5^2, <,> its bilinear
+// form: the Maxwell candidate wins exactly when Q > 0.  Q carries no
+// cancellation (for a small increment q ~ x and Q ~ 4 J(q)), so its FP32
+// value decides the comparison wherever f2^2 tmp |Q| clears the FP64
+// comparison's own roundings, even in cold elements whose relaxation tmp
+// (~1e-8 per step) lies below FP32's resolution of the stress.
+//   Inputs: xf, yf, qf the FP32 forms of x, y, q (per component, xf within
+// 2^-24 |xf| of x plus 2^-50 S for the FP64 mean; yf, formed from FP32
+// strain increments, within 2^-22 (|yf| + Y) of the FP64 y, Y = 2G sum
+// |de_i|; qf within the sum of both plus 2^-24 |qf|).  The bound on
+// |Q_est - Q| sums, per component with weights 1 (normal) and 2 (shear),
+// the first-order terms of those errors in J(q), <q, x> and J(x) with their
+// squares, and 2^-20 of the absolute terms for Q's own FP32 evaluation.
+// R bounds the FP64 side: two second_invariant2_ evaluations (each within
+// 12 u J + 12.25 u S sqrt(J) + 37.5 u^2 S^2, j2_est3's analysis) and the
+// candidates' roundings (2 u S per component), taken as 2^-45 J + 2^-45 S
+// sqrt(J) + (2^-46 S)^2 with J ~ Jq (margins of 8 and more), and the FP32 rounding of f2 - 1 in maxwell_coef
+// (2^-23 tmp relative, times J(q) + 2 tmp |<q, x>| + tmp^2 J(x), taken as
+// 2^-20 tmp of the absolute terms).  Returns 1 (Maxwell), 0 (elasto-
+// plastic: not svII < spII, ties included) or -1 (undecided, or tmp not
+// positive, or a non-finite input).
+__device__ __forceinline__ int evp_choice_f(const float *xf, const float *yf, const float *qf, float tf, float Y,
+                                            float S)
+{
+    const float e64 = 0x1p-50f * S;
+    float jq2 = 0.0f, jx2 = 0.0f, c2 = 0.0f, Aqx = 0.0f, Eqq = 0.0f, Eqx = 0.0f, Exx = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const float wt = c < 3 ? 1.0f : 2.0f;
+        const float aq = fabsf(qf[c]), ax = fabsf(xf[c]);
+        jq2 += wt * qf[c] * qf[c];
+        jx2 += wt * xf[c] * xf[c];
+        c2 += wt * qf[c] * xf[c];
+        Aqx += wt * aq * ax;
+        const float ex = 0x1p-24f * ax + e64;
+        const float eq = ex + 0x1p-22f * (fabsf(yf[c]) + Y) + 0x1p-24f * aq;
+        Eqq += wt * eq * (2.0f * aq + eq);
+        Eqx += wt * (eq * ax + ex * aq + eq * ex);
+        Exx += wt * ex * (2.0f * ax + ex);
+    }
+    const float Q = 0.5f * (2.0f + tf) * jq2 + c2 - 0.5f * tf * jx2;
+    const float absQ = (2.0f + tf) * jq2 + Aqx + tf * jx2;
+    const float EQ = 0.5f * (2.0f + tf) * Eqq + Eqx + 0.5f * tf * Exx + 0x1p-20f * absQ;
+    const float f2 = 1.0f / (1.0f + tf);
+    const float G = f2 * f2 * tf;
+    const float h = 0x1p-46f * S;
+    const float R = 0x1p-46f * jq2 + 0x1p-46f * S * sqrtf(2.0f * jq2) + h * h + 0x1p-20f * tf * absQ + 0x1p-100f;
+    if (!(tf > 0.0f)) return -1;
+    if (G * (Q - EQ) > R) return 1;
+    if (G * (Q + EQ) < -R) return 0;
+    return -1;
+}
+
 // relative volume change (rheology.cxx:569,600: vol / vol_old - 1) as
 // (vol - vol_old) (1 / vol_old): the difference is exact for volumes within a
 // factor 2 of each other, and recip_newton's ~1e-14 relative error scales the
@@ -144,6 +242,50 @@ __device__ __forceinline__ double dvol_mixed(const KP &p, int e)
 {
     const double vo = p.vol_old[e];
     return (p.vol[e] - vo) * recip_newton(vo);
+}
+
+// The mixed EVP branch where the FP32 screens leave it to FP64: the FP64
+// candidates -- the trial as the EP branch forms it (through the return map
+// unless the yield screen passed it) and the Maxwell update with FP64 terms
+// -- and, for an undecided choice (vless < 0), their FP64 comparison.  Out
+// of line: the elements that need it are few (yielding or near-tied), and
+// the registers of the return map stay out of the common path.
+__device__ __noinline__ unsigned evp_fp64_candidates(const KP &p, int e, double dt, double bulkm, double shearm,
+                                                     double visc, double s0, bool elastic, int vless, double amc,
+                                                     double anphi, double anpsi, double hardn, double ten_max,
+                                                     const double *edot, double *s, double &pls, double &dpls)
+{
+    unsigned bits = 0;
+    double de[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) de[i] = edot[i] * dt;
+    const double dev = div3((de[0] + de[1]) + de[2]);
+    const double g2 = 2 * shearm;
+    double x[3], y[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        x[i] = s[i] - s0;
+        y[i] = g2 * (de[i] - dev);
+    }
+    double sp[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) sp[i] = s[i];
+    elastic_mixed(bulkm, shearm, de, sp);
+    double depls = 0;
+    if (!elastic && mc_return_<3>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp))
+        bits |= DES_DEV_QL_NOCONV;
+    double sv[6];
+    if (vless < 0) {
+        maxwell_mixed_xy(maxwell_coef(shearm, visc, dt), g2, s0 + bulkm * dvol_mixed(p, e), x, y, s, de, sv);
+        vless = second_invariant2_<3>(sv) < second_invariant2_<3>(sp);
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s[i] = vless ? sv[i] : sp[i];
+    if (!vless) {
+        pls += depls;
+        dpls = depls;
+    }
+    return bits;
 }
 
 // update_stress (rheology.cxx:510-646), 3D, mixed precision
@@ -178,13 +320,17 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
 #pragma unroll
         for (int i = 0; i < 3; ++i) edot[i] += corr;
     }
-    double de[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        de[i] = edot[i] * dt;
-        es[i] += de[i];
-    }
     const int rt = p.mat.rheol_type;
+    double de[6];
+    if (rt != DES_RH_EVP) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            de[i] = edot[i] * dt;
+            es[i] += de[i];
+        }
+    }
+    double dpv = 0;   // dpressure
+    bool dp_set = false;
     const double bulkm = m_bulkm(p, e), shearm = m_shearm(p, e);
     const double T = elem_avg_T<4>(p, e);
     unsigned bits = 0;
@@ -209,70 +355,67 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
     } else {   // EVP: the smaller second invariant wins (rheology.cxx:594-634)
         double amc, anphi, anpsi, hardn, ten_max;
         m_plastic_props(p, e, pls, amc, anphi, anpsi, hardn, ten_max);
-        // The two candidates share the old normal deviator x_i = s_i - s0
-        // and y_i = 2G (de_i - tr(de)/3).  The elastic trial stress has the
-        // deviator x + y up to roundings: with u = 2^-53 and S = |s0| +
-        // sum |x_i| + sum |y_i| + (2G + 2K) sum |de_i| (normal components),
-        // qt = x + y lies within 22 u S of the exact deviator of the FP64
-        // trial stress that elastic_mixed forms, and s0 + K tr(de) within
-        // 12 u S of its mean.  The yield screen and the J2 estimate run on qt,
-        // with that distance added to their bounds, so the FP64 trial stress
-        // is formed only for an element that they leave undecided or that
-        // the elasto-plastic candidate wins.  The Maxwell update uses the
-        // same x and y.
-        const double trde = de[0] + de[1] + de[2];
+        // FP32 strain increments; the strain accumulates them in FP64
+        const float dtf = f32_of(dt);
+        float def[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            def[i] = f32_of(edot[i]) * dtf;
+            es[i] += f64_of(def[i]);
+        }
         const double s0 = div3(old_s);
-        const double dev = div3(trde);
-        const double g2 = 2 * shearm;
-        double x[3], y[3], qt[3], sh[3];
+        const float g2f = 2.0f * f32_of(shearm), kf = f32_of(bulkm);
+        const float trdef = (def[0] + def[1]) + def[2];
+        const float devf = trdef * (1.0f / 3.0f);
+        // x: the old deviator; y: the trial's deviatoric increment
+        float xf[6], yf[6];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            x[i] = s[i] - s0;
-            y[i] = g2 * (de[i] - dev);
-            qt[i] = x[i] + y[i];
-            sh[i] = fma(g2, de[i + 3], s[i + 3]);   // the trial's shear components, as elastic_mixed forms them
+            xf[i] = f32_of(s[i] - s0);
+            yf[i] = g2f * (def[i] - devf);
+            xf[i + 3] = f32_of(s[i + 3]);
+            yf[i + 3] = g2f * def[i + 3];
         }
-        double sv[6];
-        maxwell_mixed_xy(maxwell_coef(shearm, visc_mixed(p, e, edot, T), dt), g2, s0 + bulkm * dvol_mixed(p, e), x,
-                         y, s, de, sv);
-        const float s0f = f32_of(s0), kf = f32_of(bulkm), ktr = kf * f32_of(trde);
-        float S = fabsf(s0f), sde = 0;
+        const double visc = visc_mixed(p, e, edot, T);
+        const MaxwellF mc = maxwell_coef_f(shearm, visc, dt);
+        const float tf = (0.5f * dtf * f32_of(shearm)) / f32_of(visc);
+        const float dmp = kf * trdef;
+        float qf[6];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            S += fabsf(f32_of(x[i])) + fabsf(f32_of(y[i]));
-            sde += fabsf(f32_of(de[i]));
-        }
-        S += 2.0f * (f32_of(g2) + fabsf(kf)) * sde;
-        const float d[6] = {f32_of(qt[0]), f32_of(qt[1]), f32_of(qt[2]), f32_of(sh[0]), f32_of(sh[1]), f32_of(sh[2])};
-        // dev_err: sqrt(3) 22 u S < 2^-46.7 S, taken as 2^-44 S
-        const bool elastic = clearly_elastic3_f(f32_of(anphi), f32_of(amc), f32_of(ten_max), s0f + ktr,
-                                                fabsf(s0f) + fabsf(ktr), d, 0x1p-44f * S);
-        int vless = elastic ? j2_less(j2_est3(sv), j2_est_near3(qt, sh, S)) : -1;
-        if (vless != 1) {
-            // the elasto-plastic candidate, exactly as the EP branch forms it
-            double sp[6];
+        for (int c = 0; c < 6; ++c) qf[c] = xf[c] + yf[c];
+        // the yield screen on the trial deviator qf: against the deviator of
+        // the FP64 trial elastic_mixed(s, de) it is off by xf's and qf's
+        // roundings and by yf's distance from the FP64 y (2^-22 of
+        // Lx + Ly + Y per component, taken as 2^-21 in the 2-norm) and by
+        // the FP64 roundings of the mean (22 u S, taken as 2^-44 S)
+        const float s0f = f32_of(s0);
+        float Y = 0.0f, Sdev = 0.0f;
 #pragma unroll
-            for (int i = 0; i < 6; ++i) sp[i] = s[i];
-            elastic_mixed(bulkm, shearm, de, sp);
-            double depls = 0;
-            if (!elastic && mc_return_<3>(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp))
-                bits |= DES_DEV_QL_NOCONV;
-            // the choice is rounding-decided in near-lithostatic elements of
-            // high viscosity (J2 of a small deviator formed from pressure-sized
-            // components), and the two candidates differ in pressure (K dv
-            // against K tr(de)): where the estimates leave it open, J2 is
-            // evaluated exactly as the FP64 step does
-            if (vless < 0) vless = second_invariant2_<3>(sv) < second_invariant2_<3>(sp);
-            if (!vless) {
+        for (int i = 0; i < 3; ++i) Y += fabsf(def[i]);
+        Y *= g2f;
 #pragma unroll
-                for (int i = 0; i < 6; ++i) s[i] = sp[i];
-                pls += depls;
-                dpls = depls;
+        for (int c = 0; c < 6; ++c) Sdev += fabsf(xf[c]) + fabsf(yf[c]);
+        Sdev += Y;
+        const float S = fabsf(s0f) + Sdev + 2.0f * fabsf(kf) * (Y / fmaxf(g2f, 1e-30f));
+        const bool elastic = clearly_elastic3_f(f32_of(anphi), f32_of(amc), f32_of(ten_max), s0f + dmp,
+                                                fabsf(s0f) + fabsf(dmp), qf, 0x1p-44f * S + 0x1p-21f * Sdev);
+        int vless = elastic ? evp_choice_f(xf, yf, qf, tf, Y, S) : -1;
+        if (vless == 1) {
+            // the Maxwell update as the old stress plus its FP32 increment
+            const float dmv = kf * dvol_f(p, e);
+            float dn = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float d = fmaf(xf[i], mc.c1, fmaf(yf[i], mc.f2, dmv));
+                s[i] += f64_of(d);
+                dn += d;
+                s[i + 3] += f64_of(fmaf(xf[i + 3], mc.c1, yf[i + 3] * mc.f2));
             }
-        }
-        if (vless) {
-#pragma unroll
-            for (int i = 0; i < 6; ++i) s[i] = sv[i];
+            dpv = f64_of(dn);
+            dp_set = true;
+        } else {
+            bits |= evp_fp64_candidates(p, e, dt, bulkm, shearm, visc, s0, elastic, vless, amc, anphi, anpsi, hardn,
+                                        ten_max, edot, s, pls, dpls);
         }
     }
 #pragma unroll
@@ -283,7 +426,7 @@ __global__ void __launch_bounds__(TPB_M) k_update_stress_mixed3(KP p, int fused)
     }
     p.pls[e] = pls;
     p.dpls[e] = dpls;
-    p.dp[e] = (s[0] + s[1] + s[2]) - old_s;
+    p.dp[e] = dp_set ? dpv : (s[0] + s[1] + s[2]) - old_s;
     if (fused && p.rho_e) {
         const double rho = m_rho_T(p, e, T);
         p.rho_e[e] = rho;

@@ -10,6 +10,17 @@
 // take the same branches as the reference.  Only the upper triangle of A is
 // read.  The QL loop keeps the published 30-sweep cap; hitting it sets
 // DES_DEV_QL_NOCONV instead of returning an unchecked -1.
+//
+// Notice for eig_cardano, eig_tridiag, eig_ql and eig_hybrid, which follow
+// the arithmetic of Kopp's dsyevc3, dsytrd3, dsyevq3 and dsyevh3 step for
+// step (the FP64 path must branch as the reference does):
+//   Copyright (C) 2006 Joachim Kopp.  The original is free software; you
+//   can redistribute it and/or modify it under the terms of the GNU Lesser
+//   General Public License as published by the Free Software Foundation;
+//   either version 2.1 of the License, or (at your option) any later
+//   version.  It is distributed WITHOUT ANY WARRANTY; without even the
+//   implied warranty of MERCHANTABILITY or FITNESS FOR A PARTICULAR PURPOSE.
+//   See the GNU Lesser General Public License for more details.
 #pragma once
 
 #include "des_common.cuh"

@@ -134,12 +134,14 @@ def test_evp_choice_screen_bit_exact(dt):
 
 
 def test_evp_choice_mixed_follows_fp64_where_decided():
-    """The mixed path's choice (FP32 screen on the trial deviator it shares
-    with the yield screen) equals the FP64 path's on every element whose two
-    candidates differ by more than 1e-7 (relative) in J2; its stress is then
-    within 1e-10 of the FP64 stress (relative to the element's largest
-    component), while a different choice would move the pressure by
-    K (dv - tr de), ~1e-5 of it."""
+    """The mixed path's choice (the FP32 identity screen, or the FP64
+    comparison of its FP64 candidates) equals the FP64 path's on every
+    element whose two candidates differ by more than 1e-7 (relative) in J2.
+    Its stress is then within the FP32 rounding of the step's increment of
+    the FP64 stress (2^-20 of the increment, relative to the element's
+    largest component, where the Maxwell update is taken as the old stress
+    plus an FP32 increment), while a different choice would move the
+    pressure by K (dv - tr de), ~1e-5 of it."""
     from dynearthsol_gb300 import capi
     dt = 2e8
     wl, st, cp = _evp_case(11, dt)
@@ -156,7 +158,9 @@ def test_evp_choice_mixed_follows_fp64_where_decided():
     assert clear.sum() > 500 and (~clear).sum() > 20, (clear.sum(), (~clear).sum())
     scale = np.abs(f64["stress"]).max(axis=1)
     err = np.abs(mix["stress"] - f64["stress"]).max(axis=1) / scale
-    assert err[clear].max() <= 1e-10, err[clear].max()
+    inc = np.abs(b).max(axis=1) + tmp * np.abs(a).max(axis=1)
+    bound = 1e-10 + 2.0 ** -20 * inc / scale
+    assert (err[clear] <= bound[clear]).all(), (err[clear] / bound[clear]).max()
 
 
 def _ep_case(seed):
