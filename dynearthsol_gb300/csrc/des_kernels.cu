@@ -612,6 +612,59 @@ __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], const TetEd
     }
 }
 
+// The mixed context's tet geometry from the edges at node 0, d_i = x_i - x_0
+// (9 FP64 differences instead of the reference formulas' 18): with the cross
+// products c1 = d2 x d3, c2 = d3 x d1, c3 = d1 x d2, the signed volume is
+// d1 . c1 / 6 (geometry.cxx:29-49 evaluates the same determinant from other
+// edges), dN_i/dx = c_i / (6 vol) for i = 1..3 and dN_0/dx = -(sum of the
+// other three), an ulp or so from compute_shape_fn's values
+// (geometry.cxx:368-455).  The determinant and every product stay FP64.
+struct RelEdges {
+    double d[3][3];   // d[i - 1][k]: component k of x_i - x_0
+};
+
+__device__ __forceinline__ RelEdges rel_edges(const double *x0, const double *x1, const double *x2, const double *x3)
+{
+    RelEdges r;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        r.d[0][k] = x1[k] - x0[k];
+        r.d[1][k] = x2[k] - x0[k];
+        r.d[2][k] = x3[k] - x0[k];
+    }
+    return r;
+}
+
+// a x b, each component one fused multiply-add and one product
+__device__ __forceinline__ void cross3(const double *a, const double *b, double *out)
+{
+    out[0] = fma(a[1], b[2], -(a[2] * b[1]));
+    out[1] = fma(a[2], b[0], -(a[0] * b[2]));
+    out[2] = fma(a[0], b[1], -(a[1] * b[0]));
+}
+
+__device__ __forceinline__ double rel_volume(const RelEdges &r)
+{
+    double c1[3];
+    cross3(r.d[1], r.d[2], c1);
+    return div6(fma(r.d[0][2], c1[2], fma(r.d[0][1], c1[1], r.d[0][0] * c1[0])));
+}
+
+__device__ __forceinline__ void rel_shape_fn(const RelEdges &r, double vol, double (*shp)[4])
+{
+    double cc[3][3];
+    cross3(r.d[1], r.d[2], cc[0]);
+    cross3(r.d[2], r.d[0], cc[1]);
+    cross3(r.d[0], r.d[1], cc[2]);
+    const double iv = recip_newton(6 * vol);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+#pragma unroll
+        for (int i = 1; i < 4; ++i) shp[k][i] = cc[i - 1][k] * iv;
+        shp[k][0] = -((shp[k][1] + shp[k][2]) + shp[k][3]);
+    }
+}
+
 // jaumann_rate_3d / _2d (fields.cxx:375-404)
 __device__ __forceinline__ void jaumann3(double *s, double dt, double w3, double w4, double w5)
 {
@@ -669,10 +722,15 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
         }
         double vol;
         TetEdges te{};
-        if (ND == 3 && (flags & (GEO_VOLUME | GEO_SHAPE))) te = tet_edges(c[0], c[1], c[2], c[NPE - 1]);
+        // a mixed context's 3D geometry works from the edges at node 0
+        const bool rel0 = ND == 3 && p.shp32 != nullptr;
+        RelEdges re{};
+        if (rel0 && (flags & (GEO_VOLUME | GEO_SHAPE))) re = rel_edges(c[0], c[1], c[2], c[NPE - 1]);
+        else if (ND == 3 && (flags & (GEO_VOLUME | GEO_SHAPE))) te = tet_edges(c[0], c[1], c[2], c[NPE - 1]);
         if (flags & GEO_COPY_OLD) p.vol_old[e] = p.vol[e];
         if (flags & GEO_VOLUME) {
-            if (ND == 3) vol = tet_volume(te);
+            if (rel0) vol = rel_volume(re);
+            else if (ND == 3) vol = tet_volume(te);
             else vol = tri_area<2>(c[0], c[1], c[2]);
             p.vol[e] = vol;
             if (!(vol > 0)) set_err(p, DES_DEV_NEG_VOLUME);
@@ -681,7 +739,11 @@ __global__ void __launch_bounds__(TPB) k_geometry(KP p, int flags)
         }
         double shp[ND][NPE];
         if (flags & GEO_SHAPE) {
-            if (p.shp32) shape_fn_elem<ND, true>(c, te, vol, shp);
+            if constexpr (ND == 3) {
+                if (rel0) rel_shape_fn(re, vol, shp);
+                else if (p.shp32) shape_fn_elem<ND, true>(c, te, vol, shp);
+                else shape_fn_elem<ND>(c, te, vol, shp);
+            } else if (p.shp32) shape_fn_elem<ND, true>(c, te, vol, shp);
             else shape_fn_elem<ND>(c, te, vol, shp);
 #pragma unroll
             for (int k = 0; k < ND; ++k)

@@ -119,3 +119,30 @@ def test_unpermuted_box_is_numbered_slab_by_slab():
     assert ((e_layer == n_layer) | (e_layer == n_layer - 1)).all()
     # both numberings are monotone in the layer
     assert (np.diff(elem_layer) >= 0).all() and (np.diff(node_layer) >= 0).all()
+
+
+def test_edges_at_node0_give_the_reference_volume_and_shape_functions():
+    """The mixed context's tet geometry (rel_volume, rel_shape_fn in
+    csrc/des_kernels.cu) restated in numpy: from d_i = x_i - x_0 and the
+    cross products c1 = d2 x d3, c2 = d3 x d1, c3 = d1 x d2, the volume
+    d1 . c1 / 6 and the derivatives c_i / (6 vol), dN_0 = -(the others),
+    agree with the reference's compute_volume and compute_shape_fn (the
+    oracle) to a few ulps on a jittered, permuted mesh."""
+    from dynearthsol_gb300.config import initial_state, make_workload
+    from oracle.oracle import Oracle
+    wl = make_workload("c1_3d_evp", cells=(4, 4, 3))
+    wl.mesh = box3d(4, 4, 3, 100e3, 100e3, 10e3, jitter=0.2, permute=True, seed=3)
+    st, cp = initial_state(wl)
+    assert Oracle(wl, st, cp).init_fields() == 0
+    x, c = wl.mesh.coord, wl.mesh.connectivity
+    p = [x[c[:, i]] for i in range(4)]
+    d1, d2, d3 = p[1] - p[0], p[2] - p[0], p[3] - p[0]
+    c1, c2, c3 = np.cross(d2, d3), np.cross(d3, d1), np.cross(d1, d2)
+    vol = np.einsum("ij,ij->i", d1, c1) / 6
+    assert (vol > 0).all()
+    assert np.abs(vol / st["volume"] - 1).max() < 1e-14
+    g = [None] + [ci / (6 * vol)[:, None] for ci in (c1, c2, c3)]
+    g[0] = -(g[1] + g[2] + g[3])
+    for k, name in enumerate(("shpdx", "shpdy", "shpdz")):
+        mine = np.stack([g[i][:, k] for i in range(4)], axis=1)
+        assert np.abs(mine - st[name]).max() <= 1e-14 * np.abs(st[name]).max(), name
