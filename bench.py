@@ -555,11 +555,13 @@ def adjoint_bench(args, stream):
     viscosity field is a seeded Gaussian random field (mean 21, sd 0.5,
     correlation length 15 km), evaluated at another draw of the field.  The
     log10-viscosity gradient is checked by fourth-order central differences
-    (steps of 0.01) at
-    `adjoint_fd` elements drawn among those whose gradient is at least 1% of
-    the largest; below that step the differences of the quasi-static
-    velocity misfit are dominated by rounding (~3e-11 of the loss, which a
-    single element's share of the gradient barely exceeds over 500 steps).
+    (steps of 0.05) at `adjoint_fd` elements drawn among those whose
+    gradient is at least a quarter of the largest.  The differences of the
+    quasi-static velocity misfit carry an absolute rounding floor (~2e-26
+    per unit step over 500 steps, from the velocity differences), which a
+    single element's share of the gradient exceeds by 1e4 only near the top
+    of the gradient's range; the fourth-order truncation at that step is
+    ~(0.05 ln 10)^4 / 30 = 6e-6 of the derivative.
     The directional derivative along the normalised gradient (unit step in
     log10 viscosity, ~1e-3 per element) carries the whole gradient's signal."""
     import torch
@@ -607,7 +609,7 @@ def adjoint_bench(args, stream):
     t_step = time.perf_counter() - t0
     g = grad[LV]
     rng = np.random.default_rng(2024)
-    cand = np.nonzero(np.abs(g) >= 0.01 * np.abs(g).max())[0]
+    cand = np.nonzero(np.abs(g) >= 0.25 * np.abs(g).max())[0]
     fd = []
     # each difference L(+) - L(-) is formed from the two runs' velocities
     # (misfit_difference), not as the difference of two nearly equal misfits
@@ -616,7 +618,7 @@ def adjoint_bench(args, stream):
             lv = lv_s.copy()
             lv[e] += t
             return win.run_vel({LV: lv})
-        d = fd5_misfit(vel_at, 1e-2, target, nodes)
+        d = fd5_misfit(vel_at, 5e-2, target, nodes)
         fd.append({"elem": int(e), "adjoint": float(g[e]), "central_fd": float(d),
                    "rel_err": float(abs(d - g[e]) / max(abs(d), abs(g[e]), 1e-300))})
     # directional derivative along the normalised gradient: the whole
@@ -663,9 +665,20 @@ def yield_adjoint_bench(args, stream):
     cohesion and friction), damping option 2, run 1000 steps until the band
     yields; then a window of K steps (checkpoint every K/5) whose loss is
     the top-surface velocity misfit against a run with the band's cohesion1
-    perturbed by +-20 %.  The gradients with respect to cohesion0/1 and
-    friction0/1 are checked by fourth-order central differences at yielding
-    elements, and along the normalised cohesion1 gradient."""
+    perturbed by +-20 %.  Checks:
+    * the window's gradients against the chain of K one-step adjoints
+      (Window.chained_gradients: each step re-run alone from the state the
+      forward reached and reversed with its end state's adjoint as the seed),
+      which is the K-step adjoint by the chain rule;
+    * the chain's last link (one step from the state at step K-1, the misfit
+      as the loss) by fourth-order central differences: 5 entries each of
+      cohesion0/1 and friction0/1 at elements yielding in that step whose
+      gradient is at least 1% of the largest, and along the normalised
+      cohesion1 gradient.
+    Over the whole window central differences are not a check: with
+    elements on the yield surface the forward's rounding (stresses near
+    1e8 Pa returned to the surface, increments near 0.1 Pa) makes the loss
+    rough at every usable step size."""
     from dynearthsol_gb300 import capi
     from dynearthsol_gb300.adjoint import (Window, fd5_misfit, surface_velocity_misfit, top_nodes,
                                            yielding_adjoint_workload)
@@ -676,13 +689,14 @@ def yield_adjoint_bench(args, stream):
     wl, c1_t, c1_s = yielding_adjoint_workload()
     st, cp = initial_state(wl)
     m = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_FP64, stream=stream.cuda_stream)
-    init = m.init_fields(st)
+    m.init_fields(st)
     m.step(1000)
     start = m.download()
     clock = m.clock()
     win = Window(m, start, clock, K, C)
     nodes = top_nodes(wl.mesh)
     C1, C0, F0, F1 = capi.EF_COHESION1, capi.EF_COHESION0, capi.EF_FRICTION0, capi.EF_FRICTION1
+    names = ((C0, "cohesion0"), (C1, "cohesion1"), (F0, "friction0"), (F1, "friction1"))
     target = win.run({C1: c1_t})["vel"]
     win.set_params({C1: c1_s})
     m.upload(win.start, clock)
@@ -698,37 +712,52 @@ def yield_adjoint_bench(args, stream):
     _, grad = m.adjoint_backward({"vel": seed}, want_start=False)
     m.sync()
     t_bwd = time.perf_counter() - t0
+    # the chain of K one-step adjoints
+    t0 = time.perf_counter()
+    fin_c, _, g_c = win.chained_gradients({"vel": seed})
+    t_chain = time.perf_counter() - t0
+    chain = {n: float(np.abs(g_c[k] - grad[k]).max() / max(np.abs(grad[k]).max(), 1e-300)) for k, n in names}
+    same_final = all(np.array_equal(fin_c[k], fin[k]) for k in ("vel", "stress", "plstrain", "coord"))
+    # the last link: one step from the state at step K-1
+    pre = Window(m, start, clock, K - 1, K - 1).run() if K > 1 else start
+    link = Window(m, pre, m.clock() if K > 1 else clock, 1, 1)
     base = {k: win.fields[k].copy() for k in (C0, C1, F0, F1)}
+    link.set_params(base)
+    fin1 = link.run()
+    y1 = np.nonzero(fin1["plstrain"] > pre["plstrain"] + 1e-12)[0]
+    _, seed1 = surface_velocity_misfit(fin1["vel"], target, nodes)
+    _, g1 = link.gradients({"vel": seed1})
     rng = np.random.default_rng(7)
     checks = []
     for key, name, h in ((C1, "cohesion1", 1e3), (C0, "cohesion0", 1e3), (F1, "friction1", 1e-2),
                          (F0, "friction0", 1e-2)):
-        g = grad[key]
-        cand = yielding[np.abs(g[yielding]) >= 0.05 * np.abs(g[yielding]).max()] if len(yielding) else []
+        g = g1[key]
+        cand = y1[np.abs(g[y1]) >= 0.01 * np.abs(g[y1]).max()] if len(y1) else []
         for e in (rng.choice(cand, size=min(5, len(cand)), replace=False) if len(cand) else []):
             def vel_at(t, e=e, key=key):
                 p = dict(base)
                 p[key] = base[key].copy()
                 p[key][e] += t
-                return win.run_vel(p)
+                return link.run_vel(p)
             d = fd5_misfit(vel_at, h, target, nodes)
             checks.append({"param": name, "elem": int(e), "adjoint": float(g[e]), "central_fd": float(d),
                            "rel_err": float(abs(d - g[e]) / max(abs(d), abs(g[e]), 1e-300))})
-    g1 = grad[C1]
-    gn = float(np.linalg.norm(g1))
-    ghat = g1 / gn
-    p_dir = dict(base)
-    dfd = fd5_misfit(lambda t: win.run_vel({**p_dir, C1: base[C1] + t * 1e4 * ghat}), 1.0, target, nodes) / 1e4
+    gl = g1[C1]
+    gn = float(np.linalg.norm(gl))
+    ghat = gl / gn
+    dfd = fd5_misfit(lambda t: link.run_vel({**base, C1: base[C1] + t * 1e3 * ghat}), 1.0, target, nodes) / 1e3
     m.close()
     return {"workload": "3d yielding band (20x20x6 cubes x 6 = 14,400 tets, per-element cohesion/friction)",
             "start_step": 1000, "window_steps": K, "checkpoint_every": C,
             "yielded_elements_in_window": int(len(yielding)), "loss": loss,
             "forward_s": t_fwd, "adjoint_s": t_bwd, "adjoint_over_forward": t_bwd / t_fwd,
-            "nonzero_gradients": {n: int((np.abs(grad[k]) > 0).sum()) for k, n in
-                                  ((C0, "cohesion0"), (C1, "cohesion1"), (F0, "friction0"), (F1, "friction1"))},
-            "fd_check": checks, "fd_max_rel_err": max((r["rel_err"] for r in checks), default=None),
-            "fd_cohesion1_direction": {"adjoint": gn, "central_fd": float(dfd),
-                                       "rel_err": float(abs(dfd - gn) / max(abs(dfd), gn))}}
+            "nonzero_gradients": {n: int((np.abs(grad[k]) > 0).sum()) for k, n in names},
+            "chain_of_one_step_adjoints": {"max_rel_diff": chain, "same_final_state": same_final,
+                                           "seconds": t_chain},
+            "last_step_yielding_elements": int(len(y1)),
+            "fd_check_last_step": checks, "fd_max_rel_err": max((r["rel_err"] for r in checks), default=None),
+            "fd_cohesion1_direction_last_step": {"adjoint": gn, "central_fd": float(dfd),
+                                                 "rel_err": float(abs(dfd - gn) / max(abs(dfd), gn))}}
 
 
 def yield_bench(args, stream):

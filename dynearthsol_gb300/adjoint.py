@@ -20,7 +20,7 @@ from . import capi
 from .config import nstr_of
 from .solver import DeviceModel
 
-STATE_FIELDS = ("coord", "vel", "temperature", "stress", "plstrain")
+STATE_FIELDS = ("coord", "vel", "temperature", "stress", "plstrain", "volume_old")
 DERIVED = ("volume", "mass", "tmass", "volume_n", "shpdx", "shpdy", "shpdz")
 
 
@@ -70,6 +70,37 @@ class Window:
     def gradients(self, seed: dict):
         """Adjoint of the window last run: (start-state adjoint, parameter gradients)."""
         return self.m.adjoint_backward(seed)
+
+    def chained_gradients(self, seed: dict):
+        """The window's adjoint as a chain of K one-step adjoints: the forward
+        one step at a time from the start (each end state downloaded), then,
+        from the last step back, each step re-run alone and reversed with the
+        adjoint of its end state as the seed; the parameter gradients are
+        summed over the steps.  This is the K-step adjoint by the chain rule,
+        formed without checkpoints or a multi-step tape, so it checks those;
+        with each one-step adjoint held to finite differences it checks a
+        window over which finite differences themselves fail (over several
+        steps with elements on the Mohr-Coulomb yield surface the forward's
+        rounding -- stresses near 1e8 Pa returned to the surface, increments
+        near 0.1 Pa -- makes the loss rough at any usable step size).
+        Returns (final state, start-state adjoint, parameter gradients)."""
+        m = self.m
+        states, clocks = [], []
+        st, clk = dict(self.start), self.clock
+        for _ in range(self.K):
+            states.append(st)
+            clocks.append(clk)
+            m.upload(st, clk)
+            m.adjoint_forward(1, 1)
+            st = {k: v for k, v in m.download().items() if k not in DERIVED}
+            clk = m.clock()
+        adj, total = seed, None
+        for k in reversed(range(self.K)):
+            m.upload(states[k], clocks[k])
+            m.adjoint_forward(1, 1)
+            adj, g = m.adjoint_backward(adj)
+            total = g if total is None else {key: total[key] + g[key] for key in g}
+        return st, adj, total
 
 
 def weighted(final: dict, seed: dict) -> float:
@@ -186,7 +217,7 @@ def state_shapes(model: DeviceModel) -> dict:
     m = model.wl.mesh
     nd, nn, ne = m.ndims, m.nnode, m.nelem
     return {"coord": (nn, nd), "vel": (nn, nd), "temperature": (nn,), "stress": (ne, nstr_of(nd)),
-            "plstrain": (ne,)}
+            "plstrain": (ne,), "volume_old": (ne,)}
 
 
 # --------------------------------------------------------------------------

@@ -402,6 +402,9 @@ int des_adjoint_backward(des_ctx *c, const des_host_state *seed, des_host_state 
         if (seed->temperature && (rc = ctx_put_field(c, seed->temperature, a.aT, c->nn, 1))) return rc;
         if (seed->stress && (rc = ctx_put_field(c, seed->stress, a.as, c->ne, 6))) return rc;
         if (seed->plstrain && (rc = ctx_put_field(c, seed->plstrain, a.apls, c->ne, 1))) return rc;
+        // the final volume_old is the volume at the last step's start: its
+        // adjoint enters that step's reverse as the next state's avolo
+        if (seed->volume_old && (rc = ctx_put_field(c, seed->volume_old, a.avolo, c->ne, 1))) return rc;
     }
     for (int seg = w->nseg - 1; seg >= 0; --seg) {
         const int k0 = seg * w->C, L = std::min(w->C, w->K - k0);
@@ -441,6 +444,8 @@ int des_adjoint_backward(des_ctx *c, const des_host_state *seed, des_host_state 
             return rc;
         if (start_adjoint->stress && (rc = ctx_get_field(c, a.as, start_adjoint->stress, c->ne, 6))) return rc;
         if (start_adjoint->plstrain && (rc = ctx_get_field(c, a.apls, start_adjoint->plstrain, c->ne, 1)))
+            return rc;
+        if (start_adjoint->volume_old && (rc = ctx_get_field(c, a.avolo, start_adjoint->volume_old, c->ne, 1)))
             return rc;
     }
     CKA(cudaMemcpyAsync(c->pool, w->final_pool, c->pool_bytes, cudaMemcpyDeviceToDevice, s));

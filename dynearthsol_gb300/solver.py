@@ -229,7 +229,7 @@ class DeviceModel:
         self._check(self.lib.des_set_params(self.ctx, C.byref(self.cs.params)))
 
     # -- reverse mode --
-    ADJOINT_FIELDS = ("coord", "vel", "temperature", "stress", "plstrain")
+    ADJOINT_FIELDS = ("coord", "vel", "temperature", "stress", "plstrain", "volume_old")
 
     def adjoint_forward(self, nsteps: int, checkpoint_every: int):
         """Run a window of nsteps steps (dt held) recording a checkpoint every
@@ -245,7 +245,7 @@ class DeviceModel:
         m = self.wl.mesh
         nd, nn, ne = m.ndims, m.nnode, m.nelem
         shapes = {"coord": (nn, nd), "vel": (nn, nd), "temperature": (nn,), "stress": (ne, nstr_of(nd)),
-                  "plstrain": (ne,)}
+                  "plstrain": (ne,), "volume_old": (ne,)}
         sd = {k: np.ascontiguousarray(seed[k], dtype=np.float64) for k in self.ADJOINT_FIELDS if k in seed}
         for k, a in sd.items():
             if a.shape != shapes[k]:

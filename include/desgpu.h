@@ -432,13 +432,14 @@ int des_write_save(des_ctx *ctx, const char *filename);
  * window's end.  It also records the tape of the window's last segment
  * (checkpoint_every + 1 step records of ~319 bytes per tet, the tape the
  * backward needs anyway).  des_adjoint_backward takes the adjoint of that
- * final state in seed (its fields coord, vel, temperature, stress and
- * plstrain, in des_host_state's layout; NULL fields are zero), recomputes
+ * final state in seed (its fields coord, vel, temperature, stress,
+ * plstrain and volume_old, in des_host_state's layout; NULL fields are
+ * zero), recomputes
  * each other segment from its checkpoint onto the tape, and runs the
  * reverse steps.  With checkpoint_every >= nsteps the window is one
  * segment and the backward recomputes nothing.  Both return DES_ENOMEM
  * when the tape does not fit in device memory.  It writes the adjoint
- * of the window's start state to the same five fields of start_adjoint
+ * of the window's start state to the same six fields of start_adjoint
  * (NULL fields, or start_adjoint NULL, are skipped) and the gradients to
  * grad, and leaves the context at the window's end.  It may be called
  * again with another seed until the next des_adjoint_forward. */

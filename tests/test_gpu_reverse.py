@@ -57,6 +57,11 @@ def _dstate(win, rng, field, scale=1e-6):
         d = rng.standard_normal(a.shape) * (ext / 10)
     elif field == "plstrain":
         d = np.where(a > 1e-3, rng.standard_normal(a.shape) * np.maximum(a, 1e-3), 0.0)
+    elif field == "volume_old":
+        # vol / vol_old - 1 moves by the relative step (its rounding, 1e-16,
+        # is the difference's floor) and the pressure by K times it (~500 Pa
+        # at 1e-8; the deviators, and so the EVP choice, do not move)
+        d = rng.standard_normal(a.shape) * a * (1e-8 / scale)
     else:
         d = rng.standard_normal(a.shape) * max(float(np.abs(a).max()), 1e-30)
     return {field: d * scale}
@@ -78,7 +83,7 @@ def test_reverse_one_step_start_state():
     win = _window(_workload(), 1, 1)
     seed = _seed(win, rng)
     worst = 0.0
-    for f in ("coord", "vel", "temperature", "stress"):
+    for f in ("coord", "vel", "temperature", "stress", "volume_old"):
         ad, fd, rel = _check(win, seed, dstate=_dstate(win, rng, f))
         print(f"  d{f:12s} adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
         worst = max(worst, rel)
@@ -215,6 +220,41 @@ def test_reverse_yielding_elasto_plastic():
         assert ad != 0 and rel <= 1e-5, (k, ad, rel)
 
 
+@pytest.mark.parametrize("rheology", ["EP", "EVP"])
+def test_reverse_yielding_window_is_the_chain_of_one_step_adjoints(rheology):
+    """Over 6 yielding steps (checkpoint every 4: one recomputed segment, one
+    taped) the window's adjoint equals the chain of six one-step adjoints,
+    each from the state the forward reached: the same final state bit for
+    bit, the same start-state adjoint and parameter gradients to summation
+    order.  The links pass the adjoint of volume_old too: the end state's
+    volume_old is the volume at the step's start, which the next step's
+    Maxwell update reads (vol / vol_old - 1).  Each link is a one-step
+    adjoint, which the one-step tests hold to central differences; over the
+    chain itself central differences have a rounding floor above the signal
+    (see test_reverse_yielding_elasto_plastic)."""
+    from dynearthsol_gb300 import capi
+    rng = np.random.default_rng(9)
+    rt = capi.RH_ELASTIC | capi.RH_PLASTIC | (capi.RH_VISCOUS if rheology == "EVP" else 0)
+    wl, win = _yield_window(rt, 6, 4)
+    seed = _seed(win, rng)
+    final = win.run()
+    s_w, g_w = win.gradients(seed)
+    fin_c, s_c, g_c = win.chained_gradients(seed)
+    for k in FIELDS:
+        np.testing.assert_array_equal(fin_c[k], final[k], err_msg=k)
+    assert "volume_old" in s_w
+    for k in s_w:
+        e = np.abs(s_c[k] - s_w[k]).max() / max(np.abs(s_w[k]).max(), 1e-300)
+        assert e <= 1e-12, (k, e)
+    yielded = final["plstrain"] > win.start["plstrain"] + 1e-12
+    for k, g in g_w.items():
+        e = np.abs(g_c[k] - g).max() / max(np.abs(g).max(), 1e-300)
+        assert e <= 1e-12, (k, e)
+    for k in (capi.EF_COHESION1, capi.EF_FRICTION1):
+        assert np.count_nonzero(g_w[k][yielded]) > 0, k
+    print(f"  {rheology}: {yielded.sum()} elements yield; chain == window")
+
+
 def test_reverse_yielding_visco_elasto_plastic_one_step():
     """The EVP branch choice with elements at yield, one step.  Over several
     steps the choice of some elements flips within the finite-difference
@@ -223,7 +263,7 @@ def test_reverse_yielding_visco_elasto_plastic_one_step():
     rng = np.random.default_rng(6)
     wl, win = _yield_window(capi.RH_ELASTIC | capi.RH_VISCOUS | capi.RH_PLASTIC, 1, 1)
     seed = _seed(win, rng)
-    for f in ("vel", "stress"):
+    for f in ("vel", "stress", "volume_old"):
         ad, fd, rel = _check(win, seed, dstate=_dstate(win, rng, f))
         print(f"  EVP d{f:8s} adjoint {ad: .9e}  fd {fd: .9e}  rel {rel:.2e}")
         assert rel <= 1e-5, (f, rel)
