@@ -436,7 +436,11 @@ def main():
                 for k in ("vel", "stress", "strain", "temperature", "plstrain", "coord", "force")}
         compare = {"fp64_value": aggregate_value(ne * args.steps, ms64 / 1e3, world), "fp64_ms_per_step": ms64 / args.steps,
                    "speedup_mixed_over_fp64": ms64 / ms,
-                   "stress_rel_l2_err_vs_fp64": l2, "gate": 1e-6,
+                   "stress_rel_l2_err_vs_fp64": l2,
+                   "gated": False,
+                   "why_not_gated": ("default damping (option 1): its copysign makes the FP64 step itself "
+                                     "diverge under one-ulp changes over ~100 steps; the gate is "
+                                     "mixed_error_gate, damping option 2"),
                    "steps_compared": args.warmup + args.steps,
                    "max_normalised_err_vs_fp64": maxn}
 

@@ -396,11 +396,13 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     add((void **)&p.shp, (size_t)ne * npe * nd * D);
     const bool mixed3 = (precision == DES_PREC_MIXED) && nd == 3;
     float *d_shp32 = nullptr, *d_hc = nullptr;
+    float4 *d_ft = nullptr;
     double *d_qv = nullptr, *d_hc64 = nullptr;
     add((void **)&d_qv, (size_t)ne * D);
     if (mixed3) {
         add((void **)&d_shp32, (size_t)ne * npe * nd * sizeof(float));
         add((void **)&d_hc, (size_t)ne * npe * sizeof(float));
+        add((void **)&d_ft, (size_t)ne * npe * 2 * sizeof(float4));
     } else {
         add((void **)&d_hc64, (size_t)ne * npe * D);
     }
@@ -463,6 +465,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     p.hc = d_hc;
     p.qv = d_qv;
     p.hc64 = d_hc64;
+    p.ft = d_ft;
     p.e_lo = 0, p.e_hi = ne, p.n_lo = 0, p.n_hi = nn, p.f_lo = 0, p.f_hi = nbf;
     p.fac_order = nullptr;
     p.tape_visc = nullptr;
@@ -1082,7 +1085,8 @@ PERFN(des_update_stress,
 PERFN(des_NMD_stress, n += launch_nmd_gather(p, s); n += launch_nmd_correct(p, s, false))
 // in a mixed context, the fused-multiply-add forms of the mixed step
 PERFN(des_update_force,
-      n += launch_facet_forces(p, s); n += launch_force(p, s, false, p.shp32 && !p.mat.is_plane_strain))
+      n += launch_facet_forces(p, s); n += launch_force_terms(p, s);
+      n += launch_force(p, s, false, p.shp32 && !p.mat.is_plane_strain))
 PERFN(des_update_velocity, n += launch_velocity(p, s, p.shp32 && !p.mat.is_plane_strain))
 PERFN(des_apply_vbcs, n += launch_vbcs(p, s))
 PERFN(des_update_coordinate, n += launch_coordinate(p, s, p.shp32 && !p.mat.is_plane_strain))

@@ -105,6 +105,10 @@ struct KP {
     float *hc;                           // [4][ne] per-element heat terms of the mixed step, or null
     double *qv;                          // [ne] per-element dvoldt term of the fused steps, or null
     double *hc64;                        // [NPE][ne] per-element heat terms of the FP64 step, or null
+    // mixed 3D step: the element's share of its nodes' forces,
+    // (sigma . dN_i/dx + buoyancy z) vol, as double-word triples, two float4
+    // per (node slot i, element e) at [2 (i ne + e)]: hi (x, y, z, 0), lo
+    float4 *ft;
     // set only by the reverse mode's forward recompute: the viscosity the
     // rheology used and the EVP branch it took (1: elasto-plastic), per element
     double *tape_visc;

@@ -13,6 +13,7 @@
 #include "des_kernels.cuh"
 #include "des_rheology.cuh"
 #include "des_bc.cuh"
+#include "des_dw.cuh"
 
 namespace des {
 
@@ -394,6 +395,90 @@ __global__ void __launch_bounds__(TPB) k_nmd_correct(KP p, int with_facets)
     }
 }
 
+// The mixed 3D step's force terms of one element (fields.cxx:291-340, the
+// element's part): for each node slot i the vector
+//   T_i = (sigma . dN_i/dx + rho g / 4 z) vol,
+// which the node gather k_force_dw3 subtracts.  Formed in double-word
+// arithmetic (des_dw.cuh) from the FP64 stress, shape functions, volume and
+// buoyancy: sigma vol first (6 products), then T_1..T_3 as dot products with
+// dN_1..3/dx, T_0 = -(T_1 + T_2 + T_3) (the four shape-function gradients of
+// a tetrahedron sum to zero: the element's stress forces balance exactly),
+// and the buoyancy term rho g / 4 vol added to every z component.  Each T is
+// within ~2^-45 of its FP64 value, relative to the terms it sums; the node
+// gather then loses nothing to the cancellation between the elements.
+__device__ __forceinline__ void force_terms_dw3(const KP &p, int e, const double *s)
+{
+    const size_t ne = p.ne;
+    double buoy = 0;
+    if (p.buoy_e) {
+        buoy = p.buoy_e[e];
+    } else if (p.prm.gravity != 0) {
+        const double rho = p.rho_e ? p.rho_e[e] : m_rho<3>(p, e);
+        buoy = rho * p.prm.gravity / 4;
+    }
+    const dw v = dw_of(p.vol[e]);
+    dw sv[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) sv[c] = dw_mul(dw_of(s[c]), v);
+    dw t[4][3];
+#pragma unroll
+    for (int i = 1; i < 4; ++i) {
+        const dw sx = dw_of(shp_at(p, 0, i, e)), sy = dw_of(shp_at(p, 1, i, e)), sz = dw_of(shp_at(p, 2, i, e));
+        t[i][0] = dw_dot3(sv[0], sx, sv[3], sy, sv[4], sz);
+        t[i][1] = dw_dot3(sv[3], sx, sv[1], sy, sv[5], sz);
+        t[i][2] = dw_dot3(sv[4], sx, sv[5], sy, sv[2], sz);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) t[0][k] = dw_neg(dw_add(dw_add(t[1][k], t[2][k]), t[3][k]));
+    const dw bv = dw_mul(dw_of(buoy), v);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        t[i][2] = dw_add(t[i][2], bv);
+        float4 *o = p.ft + 2 * ((size_t)i * ne + e);
+        o[0] = make_float4(t[i][0].hi, t[i][1].hi, t[i][2].hi, 0.0f);
+        o[1] = make_float4(t[i][0].lo, t[i][1].lo, t[i][2].lo, 0.0f);
+    }
+}
+
+// k_nmd_correct<3> for the mixed step, which also forms the element's force
+// terms from the corrected stress (the same bits of stress as k_nmd_correct)
+__global__ void __launch_bounds__(TPB) k_nmd_correct_ft3(KP p, int with_facets)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, nel = p.e_hi - p.e_lo;
+    if (t < nel) {
+        const int e = p.e_lo + t;
+        const size_t ne = p.ne;
+        double dpn = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dpn += p.ntmp[conn_at(p, i, e)];
+        const double dp_el = dpn / 4;
+        const double dp_orig = p.dp[e];
+        double s[6];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            s[i] = p.stress[(size_t)i * ne + e] + divnd<3>(-dp_orig + dp_el);
+            p.stress[(size_t)i * ne + e] = s[i];
+        }
+#pragma unroll
+        for (int i = 3; i < 6; ++i) s[i] = p.stress[(size_t)i * ne + e];
+        force_terms_dw3(p, e, s);
+    } else if (with_facets && t < nel + (p.f_hi - p.f_lo)) {
+        const int i = p.f_lo + (t - nel);
+        facet_force<3>(p, p.fac_order ? p.fac_order[i] : i);
+    }
+}
+
+// the force terms alone (des_update_force in a mixed context)
+__global__ void __launch_bounds__(TPB) k_force_terms3(KP p)
+{
+    const int e = p.e_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.e_hi) return;
+    double s[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) s[c] = p.stress[(size_t)c * p.ne + e];
+    force_terms_dw3(p, e, s);
+}
+
 template <int ND>
 __global__ void __launch_bounds__(TPB) k_facet_forces(KP p)
 {
@@ -439,6 +524,9 @@ __device__ __forceinline__ double madd(double a, double b, double c)
 // f -= t * vol one fma), and dt f / m as dt f (1/m) with one recip_newton.
 // Rounding moves by an ulp of each force term, far below the FP32 strain
 // rate terms of the same step.
+template <int ND, bool CONTRACT>
+__device__ __forceinline__ void force_tail(const KP &p, int n, double *f, int fused_motion);
+
 template <int ND, bool CONTRACT = false>
 __global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
 {
@@ -481,6 +569,15 @@ __global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
             f[ND - 1] = madd<CONTRACT>(-tz, vol, f[ND - 1]);
         }
     }
+    force_tail<ND, CONTRACT>(p, n, f, fused_motion);
+}
+
+// k_force after its element gather: the gravity-induced stress BCs, the
+// elastic foundation, damping and the force store, then (fused_motion) the
+// velocity update, velocity BCs and coordinate update
+template <int ND, bool CONTRACT>
+__device__ __forceinline__ void force_tail(const KP &p, int n, double *f, int fused_motion)
+{
     // gravity-induced stress BCs, in the reference's facet order
     for (int q = p.nf_off[n]; q < p.nf_off[n + 1]; ++q) {
         int fq = p.nf_ent[q];
@@ -522,6 +619,29 @@ __global__ void __launch_bounds__(TPB) k_force(KP p, int fused_motion)
         bad |= !isfinite(xn) || !isfinite(v[d]);
     }
     if (bad) set_err(p, DES_DEV_NONFINITE);
+}
+
+// update_force of the mixed 3D step: each node sums the force terms T of its
+// support (k_nmd_correct_ft3 / k_force_terms3) in ascending element order in
+// double-word arithmetic -- whose sums are accurate relative to the exact
+// sum (Algorithm 6 of des_dw.cuh), however much the elements' terms cancel
+// -- and rounds the sum to FP64 once; the rest is k_force's FP64 tail.
+__global__ void __launch_bounds__(TPB) k_force_dw3(KP p, int fused_motion)
+{
+    const int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.n_hi) return;
+    const size_t ne = p.ne;
+    dw a0{0.0f, 0.0f}, a1{0.0f, 0.0f}, a2{0.0f, 0.0f};
+    for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+        const int ent = p.sup_ent[q];
+        const size_t o = 2 * ((size_t)(ent & 3) * ne + (ent >> 2));
+        const float4 h = __ldg(p.ft + o), l = __ldg(p.ft + o + 1);
+        a0 = dw_add(a0, {h.x, l.x});
+        a1 = dw_add(a1, {h.y, l.y});
+        a2 = dw_add(a2, {h.z, l.z});
+    }
+    double f[3] = {-f64_of(a0), -f64_of(a1), -f64_of(a2)};
+    force_tail<3, true>(p, n, f, fused_motion);
 }
 
 // CONTRACT: the form of k_force<ND, true>'s fused velocity update
@@ -1220,7 +1340,18 @@ int launch_nmd_gather(const KP &p, cudaStream_t s)
 int launch_nmd_correct(const KP &p, cudaStream_t s, bool with_facets)
 {
     long long n = (long long)(p.e_hi - p.e_lo) + (with_facets ? p.f_hi - p.f_lo : 0);
+    if (uses_force_terms(p)) {
+        k_nmd_correct_ft3<<<nblocks(n), TPB, 0, s>>>(p, (int)with_facets);
+        return 1;
+    }
     DISPATCH(k_nmd_correct, nblocks(n), p, (int)with_facets);
+    return 1;
+}
+
+int launch_force_terms(const KP &p, cudaStream_t s)
+{
+    if (!uses_force_terms(p)) return 0;
+    k_force_terms3<<<nblocks(p.e_hi - p.e_lo), TPB, 0, s>>>(p);
     return 1;
 }
 
@@ -1233,6 +1364,10 @@ int launch_facet_forces(const KP &p, cudaStream_t s)
 
 int launch_force(const KP &p, cudaStream_t s, bool fused_motion, bool contract)
 {
+    if (contract && uses_force_terms(p)) {
+        k_force_dw3<<<nblocks(p.n_hi - p.n_lo), TPB, 0, s>>>(p, (int)fused_motion);
+        return 1;
+    }
     if (contract) {
         if (p.nd == 3) k_force<3, true><<<nblocks(p.n_hi - p.n_lo), TPB, 0, s>>>(p, (int)fused_motion);
         else k_force<2, true><<<nblocks(p.n_hi - p.n_lo), TPB, 0, s>>>(p, (int)fused_motion);

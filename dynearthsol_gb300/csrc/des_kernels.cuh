@@ -32,9 +32,16 @@ int launch_node_pass(const KP &p, cudaStream_t s, bool heat);
 int launch_edvoldt(const KP &p, cudaStream_t s);
 int launch_update_stress(const KP &p, cudaStream_t s, bool fused);
 int launch_nmd_gather(const KP &p, cudaStream_t s);               // dp_nd -> ntmp
+// in a mixed 3D context (uses_force_terms) it also forms the element force
+// terms p.ft from the corrected stress, which launch_force's gather sums
 int launch_nmd_correct(const KP &p, cudaStream_t s, bool with_facets);
+// the force terms alone, from the current stress (mixed 3D contexts; else 0 launches)
+int launch_force_terms(const KP &p, cudaStream_t s);
+// a mixed 3D context's force: element terms in double-word arithmetic
+inline bool uses_force_terms(const KP &p) { return p.ft != nullptr && p.nd == 3 && !p.mat.is_plane_strain; }
 int launch_facet_forces(const KP &p, cudaStream_t s);
-// contract: the mixed step's fused multiply-add form (see k_force)
+// contract: the mixed step's form: with uses_force_terms, the double-word
+// gather of the force terms (k_force_dw3), else k_force's fused multiply-adds
 int launch_force(const KP &p, cudaStream_t s, bool fused_motion, bool contract = false);
 int launch_velocity(const KP &p, cudaStream_t s, bool contract = false);
 int launch_vbcs(const KP &p, cudaStream_t s);

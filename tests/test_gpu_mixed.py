@@ -107,3 +107,49 @@ def test_gpu_mixed_fused_equals_function_sequence():
     sa, sb = a.download(), b.download()
     for k in ("coord", "vel", "stress", "strain", "temperature", "plstrain"):
         np.testing.assert_array_equal(sa[k], sb[k], err_msg=k)
+
+
+def test_gpu_mixed_force_double_word_vs_fp64():
+    """update_force in a mixed context (element terms T = (sigma . dN/dx +
+    rho g / 4 z) vol in double-word FP32 arithmetic, summed per node in
+    double-word) against the FP64 context's update_force on the same state:
+    per node and component, |f_mixed - f_fp64| <= 2^-42 sum |T| over the
+    node's element-node pairs -- the cancellation between the elements'
+    terms (lithostatic stresses of ~1e8 Pa against the small net force)
+    leaves the double-word sums accurate to the ~2^-45 of their terms, where
+    FP32 products would lose everything below 2^-24 of them."""
+    from dataclasses import replace
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import initial_state, make_workload
+    from dynearthsol_gb300.solver import DeviceModel
+    wl = make_workload("c1_3d_evp", cells=(12, 12, 4))
+    wl.params = replace(wl.params, damping_option=2)
+    st, cp = initial_state(wl)
+    f64 = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_FP64)
+    f64.init_fields(st)
+    f64.step(30)
+    state, clk = f64.download(), f64.clock()
+    mix = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_MIXED)
+    mix.upload({k: v.copy() for k, v in state.items()}, clk)
+    f64.upload({k: v.copy() for k, v in state.items()}, clk)
+    f64.call("update_force")
+    mix.call("update_force")
+    fa, fb = f64.download()["force"], mix.download()["force"]
+    # sum over each node's (element, slot) pairs of |sigma| . |dN/dx| vol + |rho g / 4| vol
+    m = wl.mesh
+    s, vol = state["stress"], state["volume"]
+    shp = np.stack([state["shpdx"], state["shpdy"], state["shpdz"]], axis=1)   # [ne, 3, 4]
+    rows = ((0, 3, 4), (3, 1, 5), (4, 5, 2))
+    g = abs(wl.params.gravity) * float(np.max(wl.mat.rho0)) / 4
+    absT = np.zeros((m.nnode, 3))
+    for i in range(4):
+        for k, (a, b, c) in enumerate(rows):
+            t = (np.abs(s[:, a]) * np.abs(shp[:, 0, i]) + np.abs(s[:, b]) * np.abs(shp[:, 1, i])
+                 + np.abs(s[:, c]) * np.abs(shp[:, 2, i]) + (g if k == 2 else 0.0)) * vol
+            np.add.at(absT[:, k], m.connectivity[:, i], t)
+    ratio = np.abs(fb - fa) / absT
+    net = np.abs(fa) / absT
+    print(f"double-word force vs FP64: max |df| / sum|T| = {ratio.max():.2e} (2^{np.log2(ratio.max()):.1f}); "
+          f"the net force is {np.median(net):.1e} of sum|T| (median)")
+    assert ratio.max() <= 2.0 ** -42, ratio.max()
+    assert np.count_nonzero(fb != fa) > 0
