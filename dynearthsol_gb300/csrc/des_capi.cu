@@ -397,12 +397,14 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     const bool mixed3 = (precision == DES_PREC_MIXED) && nd == 3;
     float *d_shp32 = nullptr, *d_hc = nullptr;
     float4 *d_ft = nullptr;
+    int *d_sup_pos = nullptr;
     double *d_qv = nullptr, *d_hc64 = nullptr;
     add((void **)&d_qv, (size_t)ne * D);
     if (mixed3) {
         add((void **)&d_shp32, (size_t)ne * npe * nd * sizeof(float));
         add((void **)&d_hc, (size_t)ne * npe * sizeof(float));
         add((void **)&d_ft, (size_t)ne * npe * 2 * sizeof(float4));
+        add((void **)&d_sup_pos, (size_t)ne * npe * I);
     } else {
         add((void **)&d_hc64, (size_t)ne * npe * D);
     }
@@ -466,6 +468,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     p.qv = d_qv;
     p.hc64 = d_hc64;
     p.ft = d_ft;
+    p.sup_pos = d_sup_pos;
     p.e_lo = 0, p.e_hi = ne, p.n_lo = 0, p.n_hi = nn, p.f_lo = 0, p.f_hi = nbf;
     p.fac_order = nullptr;
     p.tape_visc = nullptr;
@@ -488,6 +491,11 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     up(d_bc, mesh->bcflag, (size_t)nn * sizeof(unsigned));
     up(d_sup_off, sup_off.data(), sup_off.size() * I);
     up(d_sup_ent, sup_ent.data(), sup_ent.size() * I);
+    if (d_sup_pos) {   // the support-list entry of each (element, slot), slot-major
+        std::vector<int> pos((size_t)ne * npe);
+        for (size_t q = 0; q < sup_ent.size(); ++q) pos[(size_t)(sup_ent[q] & 3) * ne + (sup_ent[q] >> 2)] = (int)q;
+        up(d_sup_pos, pos.data(), pos.size() * I);
+    }
     up(d_nf_off, nf_off.data(), nf_off.size() * I);
     up(d_nf_ent, nf_ent.data(), nf_ent.size() * I);
     up(d_fe, fac_elem.data(), fac_elem.size() * I);

@@ -107,8 +107,10 @@ struct KP {
     double *hc64;                        // [NPE][ne] per-element heat terms of the FP64 step, or null
     // mixed 3D step: the element's share of its nodes' forces,
     // (sigma . dN_i/dx + buoyancy z) vol, as double-word triples, two float4
-    // per (node slot i, element e) at [2 (i ne + e)]: hi (x, y, z, 0), lo
+    // (hi (x, y, z, 0), lo) per support-list entry, at [2 q] for the entry q
+    // of (element e, slot i): q = sup_pos[i ne + e], the inverse of sup_ent
     float4 *ft;
+    const int *sup_pos;
     // set only by the reverse mode's forward recompute: the viscosity the
     // rheology used and the EVP branch it took (1: elasto-plastic), per element
     double *tape_visc;

@@ -16,7 +16,11 @@
 //     Algorithm 6 (AccurateDWPlusDW): relative error below 3u^2 + 13u^3 of the
 //     exact sum, cancellation included;
 //   * dw_mul: the same paper, Algorithm 12 (DWTimesDW3): relative error
-//     below 4u^2.
+//     below 4u^2;
+//   * dw_dot3, dw_sum3: the compensated dot product and sum Dot2 / Sum2 of
+//     Ogita, Rump, Oishi, "Accurate sum and dot product", SIAM J. Sci.
+//     Comput. 26(6), 2005, on the high parts, with the low parts' terms
+//     added to the compensation.
 // The library is compiled with --fmad=false: no multiply and add below is
 // contracted beyond the fmaf calls written out.
 #pragma once
@@ -98,6 +102,59 @@ __device__ __forceinline__ dw dw_of(double x)
     if (mag < (897u << 20) || mag >= (1151u << 20)) l = 0.0f;
     l = __int_as_float(__float_as_int(l) ^ (int)(hw & 0x80000000u));
     return {h, l};
+}
+
+// The double-word form of an FP64 value by truncation, cheaper than dw_of:
+// hi = x's sign, exponent and top 23 stored significand bits (x truncated to
+// 24 significant bits), lo = the remaining 29 bits, of x's sign, rounded to
+// float by one integer-to-float conversion and scaled by a power of two.
+// |lo| < ulp(hi) and |x - (hi + lo)| <= 2^-47 |x|.  For |x| in [2^-126,
+// 2^128); smaller magnitudes give (0, 0), larger ones and NaN (inf / NaN, 0).
+__device__ __forceinline__ dw dw_split(double x)
+{
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const unsigned mag = hw & 0x7fffffffu, sg = hw & 0x80000000u;
+    unsigned hb = ((mag - (896u << 20)) << 3) | (lw >> 29);
+    const float fr = __uint2float_rn(lw & 0x1fffffffu);
+    const int ef = (int)(mag >> 20) - 948;   // biased FP32 exponent of 2^(E - 52)
+    float l = ef >= 1 ? fr * __uint_as_float((unsigned)ef << 23)
+                      : (fr * __uint_as_float((unsigned)(ef + 64) << 23)) * 0x1p-64f;
+    if (mag < (897u << 20)) {
+        hb = 0;
+        l = 0.0f;
+    } else if (mag >= (1151u << 20)) {
+        hb = (mag > 0x7ff00000u || (mag == 0x7ff00000u && lw)) ? 0x7fc00000u : 0x7f800000u;
+        l = 0.0f;
+    }
+    return {__uint_as_float(sg | hb), __uint_as_float(__float_as_uint(l) ^ sg)};
+}
+
+// a0 b0 + a1 b1 + a2 b2 for double-word operands: Dot2 on the high parts
+// (exact products by two_prod, exact sums by two_sum, their errors summed in
+// one float s), the cross terms ah bl + al bh added to s, al bl (below
+// u^2 |a b|) dropped, and the pair (sum, s) renormalised.  The error is at
+// most about (gamma_3^2 + 3u^2) sum |a_i b_i| ~ 12u^2 of the terms' magnitudes,
+// however much they cancel: 37 operations against dw_dot3's 67.
+__device__ __forceinline__ dw dw_dot3c(dw a0, dw b0, dw a1, dw b1, dw a2, dw b2)
+{
+    const dw p0 = two_prod(a0.hi, b0.hi), p1 = two_prod(a1.hi, b1.hi), p2 = two_prod(a2.hi, b2.hi);
+    float s = p0.lo + fmaf(a0.hi, b0.lo, a0.lo * b0.hi);
+    const dw t1 = two_sum(p0.hi, p1.hi);
+    s += t1.lo + (p1.lo + fmaf(a1.hi, b1.lo, a1.lo * b1.hi));
+    const dw t2 = two_sum(t1.hi, p2.hi);
+    s += t2.lo + (p2.lo + fmaf(a2.hi, b2.lo, a2.lo * b2.hi));
+    return two_sum(t2.hi, s);
+}
+
+// x + y + z of double-word values: Sum2 on the high parts with the low parts
+// added to the compensation; error about 4u^2 (|x| + |y| + |z|)
+__device__ __forceinline__ dw dw_sum3(dw x, dw y, dw z)
+{
+    const dw t1 = two_sum(x.hi, y.hi);
+    float c = t1.lo + (x.lo + y.lo);
+    const dw t2 = two_sum(t1.hi, z.hi);
+    c += t2.lo + z.lo;
+    return two_sum(t2.hi, c);
 }
 
 // hi + lo rounded to FP64 (one FP64 addition; both conversions are exact)

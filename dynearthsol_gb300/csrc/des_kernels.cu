@@ -400,12 +400,13 @@ __global__ void __launch_bounds__(TPB) k_nmd_correct(KP p, int with_facets)
 //   T_i = (sigma . dN_i/dx + rho g / 4 z) vol,
 // which the node gather k_force_dw3 subtracts.  Formed in double-word
 // arithmetic (des_dw.cuh) from the FP64 stress, shape functions, volume and
-// buoyancy: sigma vol first (6 products), then T_1..T_3 as dot products with
-// dN_1..3/dx, T_0 = -(T_1 + T_2 + T_3) (the four shape-function gradients of
-// a tetrahedron sum to zero: the element's stress forces balance exactly),
-// and the buoyancy term rho g / 4 vol added to every z component.  Each T is
-// within ~2^-45 of its FP64 value, relative to the terms it sums; the node
-// gather then loses nothing to the cancellation between the elements.
+// buoyancy: sigma vol first (6 products), then T_1..T_3 as compensated dot
+// products with dN_1..3/dx, T_0 = -(T_1 + T_2 + T_3) (the four shape-function
+// gradients of a tetrahedron sum to zero: the element's stress forces
+// balance exactly), and the buoyancy term rho g / 4 vol added to every z
+// component.  Each T is within ~2^-44 of its FP64 value, relative to the
+// terms it sums.  T_i goes to the support-list entry of (e, i), so that
+// each node's gather reads its terms from consecutive memory.
 __device__ __forceinline__ void force_terms_dw3(const KP &p, int e, const double *s)
 {
     const size_t ne = p.ne;
@@ -416,25 +417,26 @@ __device__ __forceinline__ void force_terms_dw3(const KP &p, int e, const double
         const double rho = p.rho_e ? p.rho_e[e] : m_rho<3>(p, e);
         buoy = rho * p.prm.gravity / 4;
     }
-    const dw v = dw_of(p.vol[e]);
+    const dw v = dw_split(p.vol[e]);
     dw sv[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) sv[c] = dw_mul(dw_of(s[c]), v);
+    for (int c = 0; c < 6; ++c) sv[c] = dw_mul(dw_split(s[c]), v);
     dw t[4][3];
 #pragma unroll
     for (int i = 1; i < 4; ++i) {
-        const dw sx = dw_of(shp_at(p, 0, i, e)), sy = dw_of(shp_at(p, 1, i, e)), sz = dw_of(shp_at(p, 2, i, e));
-        t[i][0] = dw_dot3(sv[0], sx, sv[3], sy, sv[4], sz);
-        t[i][1] = dw_dot3(sv[3], sx, sv[1], sy, sv[5], sz);
-        t[i][2] = dw_dot3(sv[4], sx, sv[5], sy, sv[2], sz);
+        const dw sx = dw_split(shp_at(p, 0, i, e)), sy = dw_split(shp_at(p, 1, i, e)),
+                 sz = dw_split(shp_at(p, 2, i, e));
+        t[i][0] = dw_dot3c(sv[0], sx, sv[3], sy, sv[4], sz);
+        t[i][1] = dw_dot3c(sv[3], sx, sv[1], sy, sv[5], sz);
+        t[i][2] = dw_dot3c(sv[4], sx, sv[5], sy, sv[2], sz);
     }
 #pragma unroll
-    for (int k = 0; k < 3; ++k) t[0][k] = dw_neg(dw_add(dw_add(t[1][k], t[2][k]), t[3][k]));
-    const dw bv = dw_mul(dw_of(buoy), v);
+    for (int k = 0; k < 3; ++k) t[0][k] = dw_neg(dw_sum3(t[1][k], t[2][k], t[3][k]));
+    const dw bv = dw_mul(dw_split(buoy), v);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         t[i][2] = dw_add(t[i][2], bv);
-        float4 *o = p.ft + 2 * ((size_t)i * ne + e);
+        float4 *o = p.ft + 2 * (size_t)p.sup_pos[(size_t)i * ne + e];
         o[0] = make_float4(t[i][0].hi, t[i][1].hi, t[i][2].hi, 0.0f);
         o[1] = make_float4(t[i][0].lo, t[i][1].lo, t[i][2].lo, 0.0f);
     }
@@ -622,7 +624,8 @@ __device__ __forceinline__ void force_tail(const KP &p, int n, double *f, int fu
 }
 
 // update_force of the mixed 3D step: each node sums the force terms T of its
-// support (k_nmd_correct_ft3 / k_force_terms3) in ascending element order in
+// support (k_nmd_correct_ft3 / k_force_terms3, stored in the support list's
+// order: one contiguous run per node) in ascending element order in
 // double-word arithmetic -- whose sums are accurate relative to the exact
 // sum (Algorithm 6 of des_dw.cuh), however much the elements' terms cancel
 // -- and rounds the sum to FP64 once; the rest is k_force's FP64 tail.
@@ -630,12 +633,9 @@ __global__ void __launch_bounds__(TPB) k_force_dw3(KP p, int fused_motion)
 {
     const int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= p.n_hi) return;
-    const size_t ne = p.ne;
     dw a0{0.0f, 0.0f}, a1{0.0f, 0.0f}, a2{0.0f, 0.0f};
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
-        const int ent = p.sup_ent[q];
-        const size_t o = 2 * ((size_t)(ent & 3) * ne + (ent >> 2));
-        const float4 h = __ldg(p.ft + o), l = __ldg(p.ft + o + 1);
+        const float4 h = __ldg(p.ft + 2 * (size_t)q), l = __ldg(p.ft + 2 * (size_t)q + 1);
         a0 = dw_add(a0, {h.x, l.x});
         a1 = dw_add(a1, {h.y, l.y});
         a2 = dw_add(a2, {h.z, l.z});
