@@ -155,12 +155,18 @@ __device__ __forceinline__ unsigned biased_exponent(double x)
     return ((unsigned)__double2hiint(x) >> 20) & 0x7ffu;
 }
 
+// the divisions of div3 and div6 for the rare operands where the product
+// form does not apply, out of line: inlined, the compiler evaluates the
+// division's whole FP64 sequence for every element and selects the result
+static __device__ __noinline__ double div3_slow(double x) { return x / 3; }
+static __device__ __noinline__ double div6_slow(double x) { return x / 6; }
+
 __device__ __forceinline__ double div3(double x)
 {
     constexpr double YH = 0x1.5555555555555p-2;    // RN(1/3)
     constexpr double YL = 0x1.5555555555555p-56;   // RN(1/3 - YH)
     const unsigned mag_hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
-    if (mag_hi < (123u << 20) && (mag_hi | (unsigned)__double2loint(x)) != 0) return x / 3;
+    if (mag_hi < (123u << 20) && (mag_hi | (unsigned)__double2loint(x)) != 0) return div3_slow(x);
     return fma(x, YH, x * YL);
 }
 
@@ -170,7 +176,7 @@ __device__ __forceinline__ double div3(double x)
 __device__ __forceinline__ double div6(double x)
 {
     const unsigned e = biased_exponent(x);
-    if (e < 123u || e == 0x7ffu) return x / 6;
+    if (e < 123u || e == 0x7ffu) return div6_slow(x);
     return div3(__hiloint2double(__double2hiint(x) - (1 << 20), __double2loint(x)));
 }
 

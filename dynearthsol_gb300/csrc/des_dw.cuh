@@ -107,7 +107,8 @@ __device__ __forceinline__ dw dw_of(double x)
 // The double-word form of an FP64 value by truncation, cheaper than dw_of:
 // hi = x's sign, exponent and top 23 stored significand bits (x truncated to
 // 24 significant bits), lo = the remaining 29 bits, of x's sign, rounded to
-// float by one integer-to-float conversion and scaled by a power of two.
+// float (2^23 + b - 2^23 gives the halves exactly, one fma joins them) and
+// scaled by a power of two.
 // |lo| < ulp(hi) and |x - (hi + lo)| <= 2^-47 |x|.  For |x| in [2^-126,
 // 2^128); smaller magnitudes give (0, 0), larger ones and NaN (inf / NaN, 0).
 __device__ __forceinline__ dw dw_split(double x)
@@ -115,7 +116,10 @@ __device__ __forceinline__ dw dw_split(double x)
     const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
     const unsigned mag = hw & 0x7fffffffu, sg = hw & 0x80000000u;
     unsigned hb = ((mag - (896u << 20)) << 3) | (lw >> 29);
-    const float fr = __uint2float_rn(lw & 0x1fffffffu);
+    // the 29 bits as a float from two exact halves (FP32 instructions only)
+    const unsigned L = lw & 0x1fffffffu;
+    const float fr = fmaf(__uint_as_float(0x4B000000u | (L >> 23)) - 8388608.0f, 8388608.0f,
+                          __uint_as_float(0x4B000000u | (L & 0x7fffffu)) - 8388608.0f);
     const int ef = (int)(mag >> 20) - 948;   // biased FP32 exponent of 2^(E - 52)
     float l = ef >= 1 ? fr * __uint_as_float((unsigned)ef << 23)
                       : (fr * __uint_as_float((unsigned)(ef + 64) << 23)) * 0x1p-64f;
