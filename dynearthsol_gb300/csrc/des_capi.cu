@@ -394,9 +394,11 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     add((void **)&p.vol, (size_t)ne * D);
     add((void **)&p.vol_old, (size_t)ne * D);
     add((void **)&p.shp, (size_t)ne * npe * nd * D);
-    const bool mixed3 = (precision == DES_PREC_MIXED) && nd == 3;
+    // the mixed step's kernels are 3D; a plane-strain material runs the FP64 ones
+    const bool mixed3 = (precision == DES_PREC_MIXED) && nd == 3 && !mat->is_plane_strain;
     float *d_shp32 = nullptr, *d_hc = nullptr;
     float4 *d_ft = nullptr;
+    float2 *d_shpdw = nullptr;
     int *d_sup_pos = nullptr;
     double *d_qv = nullptr, *d_hc64 = nullptr;
     add((void **)&d_qv, (size_t)ne * D);
@@ -404,6 +406,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
         add((void **)&d_shp32, (size_t)ne * npe * nd * sizeof(float));
         add((void **)&d_hc, (size_t)ne * npe * sizeof(float));
         add((void **)&d_ft, (size_t)ne * npe * 2 * sizeof(float4));
+        add((void **)&d_shpdw, (size_t)ne * npe * nd * sizeof(float2));
         add((void **)&d_sup_pos, (size_t)ne * npe * I);
     } else {
         add((void **)&d_hc64, (size_t)ne * npe * D);
@@ -464,6 +467,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     p.buoy_e = nullptr;
     p.tdot = p.ntmp;
     p.shp32 = d_shp32;
+    p.shpdw = d_shpdw;
     p.hc = d_hc;
     p.qv = d_qv;
     p.hc64 = d_hc64;
@@ -826,6 +830,9 @@ int download_state(des_ctx *c, des_host_state *st, bool early, bool after_step =
         for (int k = 0; k < nf; ++k)
             if (f[k].early && (rc = pp.field(f[k].host, f[k].dev, f[k].n, f[k].ncomp, true))) return rc;
     }
+    // a mixed context keeps its shape functions as double-word pairs
+    if ((out.shpdx || out.shpdy || out.shpdz) && (rc = check_launch(c, launch_shp_join(c->kp, c->stream))))
+        return rc;
     if ((rc = pp.begin())) return rc;
     for (int k = 0; k < nf; ++k)
         if (!(early && f[k].early) && (rc = pp.field(f[k].host, f[k].dev, f[k].n, f[k].ncomp))) return rc;
@@ -856,7 +863,7 @@ int des_upload_state(des_ctx *c, const des_host_state *st)
     des_host_state in = *st;
     const bool have_shp = st->shpdx && st->shpdz && (nd == 2 || st->shpdy);
     const bool have_mass = st->mass && st->tmass && st->volume_n;
-    if (!have_shp) in.shpdx = in.shpdy = in.shpdz = nullptr;
+    if (!have_shp || p.shpdw) in.shpdx = in.shpdy = in.shpdz = nullptr;
     if (!have_mass) in.mass = in.tmass = in.volume_n = nullptr;
     StateField f[MAX_STATE_FIELDS];
     const int nf = state_fields(c, &in, f);
@@ -888,10 +895,12 @@ int des_upload_state(des_ctx *c, const des_host_state *st)
     }
     KP q = p;   // per-function form
     if (!st->volume && (rc = check_launch(c, launch_geometry(q, c->stream, GEO_VOLUME)))) return rc;
-    if (have_shp) {
-        if (p.shp32 && (rc = check_launch(c, launch_f64_to_f32(p.shp, p.shp32, (long long)ne * npe * nd, c->stream))))
-            return rc;
-    } else if ((rc = check_launch(c, launch_geometry(q, c->stream, GEO_SHAPE)))) return rc;
+    // a mixed 3D context forms its double-word shape functions from the
+    // coordinates: FP64 values do not split into pairs exactly, and so do not
+    // carry its own pairs through a download and an upload
+    if (!have_shp || p.shpdw) {
+        if ((rc = check_launch(c, launch_geometry(q, c->stream, GEO_SHAPE)))) return rc;
+    }
     if (!have_mass && (rc = check_launch(c, launch_mass(q, c->stream)))) return rc;
     CK(cudaStreamSynchronize(c->stream));
     c->has_state = true;
@@ -969,6 +978,8 @@ int transfer_fields(des_ctx *c, des_host_state *st, unsigned mask, bool up)
     int rc;
     if ((rc = ensure_xfer(c))) return rc;
     Pipe pp{c, up};
+    // a mixed context keeps its shape functions as double-word pairs
+    if ((mask & DES_F_SHP) && !up && (rc = check_launch(c, launch_shp_join(c->kp, c->stream)))) return rc;
     if ((rc = pp.begin())) return rc;
     for (const FieldDesc &fd : kFields) {
         if (!(mask & fd.bit)) continue;
@@ -990,9 +1001,8 @@ int transfer_fields(des_ctx *c, des_host_state *st, unsigned mask, bool up)
         }
     }
     if ((rc = pp.end())) return rc;
-    if ((mask & DES_F_SHP) && up && c->kp.shp32) {   // keep the FP32 copy of the mixed step in step
-        rc = check_launch(c, launch_f64_to_f32(c->kp.shp, c->kp.shp32, (long long)c->ne * c->npe * c->nd,
-                                               c->stream));
+    if ((mask & DES_F_SHP) && up && c->kp.shpdw) {   // a mixed 3D context forms them from its coordinates
+        rc = check_launch(c, launch_geometry(c->kp, c->stream, GEO_SHAPE));
         if (rc) return rc;
     }
     if (mask & DES_F_CLOCK) {
@@ -1289,6 +1299,7 @@ struct SlabField {
     int ncomp;
     bool node, up, down;
     double *stage;
+    const float2 *dw;   // download from these double-word pairs instead of dev (mixed shape functions)
 };
 
 // The fields of one call, or false when the call does not qualify: the
@@ -1306,6 +1317,7 @@ bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &o
     const int nd = c->nd, npe = c->npe, nstr = c->nstr, ne = c->ne;
     const size_t shp1 = (size_t)ne * npe;
     float *s32 = use_mixed(c) ? p.shp32 : nullptr;
+    const float2 *dw = p.shpdw;
     const bool ps = p.mat.is_plane_strain != 0;
     const bool qs = p.prm.is_quasi_static != 0;
     // up: needed by the step; down: written by it (strain_rate, force,
@@ -1331,10 +1343,11 @@ bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &o
         {st->stressyy, p.syy, nullptr, 1, false, true, ps, nullptr},
         {st->dpressure, p.dp, nullptr, 1, false, false, true, nullptr},
         {st->edvoldt, p.edvoldt, nullptr, 1, false, false, true, nullptr},
-        {st->shpdx, p.shp, s32, npe, false, false, true, nullptr},
-        {nd == 3 ? st->shpdy : nullptr, p.shp + shp1, s32 ? s32 + shp1 : nullptr, npe, false, false, nd == 3, nullptr},
+        {st->shpdx, p.shp, s32, npe, false, false, true, nullptr, dw},
+        {nd == 3 ? st->shpdy : nullptr, p.shp + shp1, s32 ? s32 + shp1 : nullptr, npe, false, false, nd == 3, nullptr,
+         dw ? dw + shp1 : nullptr},
         {st->shpdz, p.shp + (size_t)(nd - 1) * shp1, s32 ? s32 + (size_t)(nd - 1) * shp1 : nullptr, npe, false, false, true,
-         nullptr},
+         nullptr, dw ? dw + (size_t)(nd - 1) * shp1 : nullptr},
     };
     out.clear();
     size_t off = 0;
@@ -1487,7 +1500,7 @@ int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec
             const int lo = f.node ? c->slab_n[flo] : c->slab_e[flo], hi = f.node ? c->slab_n[fhi] : c->slab_e[fhi];
             if (hi <= lo) continue;
             RowField &r = t.f[t.count++];
-            r = {f.stage, f.dev, nullptr, t.total, f.node ? c->nn : c->ne, f.ncomp, lo, hi};
+            r = {f.stage, f.dev, nullptr, t.total, f.node ? c->nn : c->ne, f.ncomp, lo, hi, f.dw};
             t.total += (long long)(hi - lo) * f.ncomp;
         }
         n += launch_rows(t, false, ys);

@@ -81,30 +81,8 @@ __device__ __forceinline__ dw dw_dot3(dw a0, dw b0, dw a1, dw b1, dw a2, dw b2)
     return dw_add(dw_add(dw_mul(a0, b0), dw_mul(a1, b1)), dw_mul(a2, b2));
 }
 
-// The double-word form of an FP64 value without an FP64 instruction: hi =
-// f32_of(x), the nearest float (ties away from zero: f32_of rounds up exactly
-// when bit 28 of the low word is set), and lo = the remainder x - hi, which is
-// the low 29 significand bits less 2^29 when hi was rounded up, in units of
-// 2^(E - 52) for x's exponent E, converted with one integer-to-float rounding
-// and scaled by a power of two built from bits.  |lo| <= ulp(hi) / 2 and
-// |x - (hi + lo)| <= 2^-48 |x|.  For |x| in [2^-126, 2^128); smaller
-// magnitudes give (0, 0), infinities and NaN give (hi, 0).
-__device__ __forceinline__ dw dw_of(double x)
-{
-    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
-    const unsigned mag = hw & 0x7fffffffu;
-    const float h = f32_of(x);
-    const int r = (int)(lw & 0x1fffffffu) - (int)((lw & 0x10000000u) << 1);
-    const float fr = __int2float_rn(r);
-    const int ef = (int)(mag >> 20) - 948;   // biased FP32 exponent of 2^(E - 52)
-    float l = ef >= 1 ? fr * __uint_as_float((unsigned)ef << 23)
-                      : (fr * __uint_as_float((unsigned)(ef + 64) << 23)) * 0x1p-64f;
-    if (mag < (897u << 20) || mag >= (1151u << 20)) l = 0.0f;
-    l = __int_as_float(__float_as_int(l) ^ (int)(hw & 0x80000000u));
-    return {h, l};
-}
-
-// The double-word form of an FP64 value by truncation, cheaper than dw_of:
+// The double-word form of an FP64 value by truncation, without an FP64
+// instruction:
 // hi = x's sign, exponent and top 23 stored significand bits (x truncated to
 // 24 significant bits), lo = the remaining 29 bits, of x's sign, rounded to
 // float (2^23 + b - 2^23 gives the halves exactly, one fma joins them) and
@@ -160,6 +138,31 @@ __device__ __forceinline__ dw dw_sum3(dw x, dw y, dw z)
     c += t2.lo + z.lo;
     return two_sum(t2.hi, c);
 }
+
+// a b - c d for double-word operands (a cross-product component), in the
+// manner of dw_dot3c: exact high products and difference, the errors and the
+// cross terms in one float; error about 5u^2 (|a b| + |c d|)
+__device__ __forceinline__ dw dw_diff2(dw a, dw b, dw c, dw d)
+{
+    const dw p = two_prod(a.hi, b.hi), q = two_prod(c.hi, d.hi);
+    const dw t = two_sum(p.hi, -q.hi);
+    const float s = ((p.lo - q.lo) + (fmaf(a.hi, b.lo, a.lo * b.hi) - fmaf(c.hi, d.lo, c.lo * d.hi))) + t.lo;
+    return two_sum(t.hi, s);
+}
+
+// 1 / x for a double-word x of normal magnitude: the FP32 quotient r0 and one
+// Newton step r0 + r0 (1 - x r0), whose residual is formed exactly up to
+// x.lo r0 (x.hi r0 by two_prod, 1 - its high part exact as it lies within
+// 2u of 1); relative error about 3u^2
+__device__ __forceinline__ dw dw_recip(dw x)
+{
+    const float r0 = 1.0f / x.hi;
+    const dw p = two_prod(x.hi, r0);
+    const float e = ((1.0f - p.hi) - p.lo) - x.lo * r0;
+    return fast_two_sum(r0, r0 * e);
+}
+
+__device__ __forceinline__ dw dw_of2(float2 v) { return {v.x, v.y}; }
 
 // hi + lo rounded to FP64 (one FP64 addition; both conversions are exact)
 __device__ __forceinline__ double f64_of(dw x) { return f64_of(x.hi) + f64_of(x.lo); }

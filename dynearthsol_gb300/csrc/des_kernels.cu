@@ -399,8 +399,8 @@ __global__ void __launch_bounds__(TPB) k_nmd_correct(KP p, int with_facets)
 // element's part): for each node slot i the vector
 //   T_i = (sigma . dN_i/dx + rho g / 4 z) vol,
 // which the node gather k_force_dw3 subtracts.  Formed in double-word
-// arithmetic (des_dw.cuh) from the FP64 stress, shape functions, volume and
-// buoyancy: sigma vol first (6 products), then T_1..T_3 as compensated dot
+// arithmetic (des_dw.cuh) from the FP64 stress, volume and buoyancy and the
+// double-word shape functions: sigma vol first (6 products), then T_1..T_3 as compensated dot
 // products with dN_1..3/dx, T_0 = -(T_1 + T_2 + T_3) (the four shape-function
 // gradients of a tetrahedron sum to zero: the element's stress forces
 // balance exactly), and the buoyancy term rho g / 4 vol added to every z
@@ -424,8 +424,8 @@ __device__ __forceinline__ void force_terms_dw3(const KP &p, int e, const double
     dw t[4][3];
 #pragma unroll
     for (int i = 1; i < 4; ++i) {
-        const dw sx = dw_split(shp_at(p, 0, i, e)), sy = dw_split(shp_at(p, 1, i, e)),
-                 sz = dw_split(shp_at(p, 2, i, e));
+        const dw sx = dw_of2(p.shpdw[(size_t)i * ne + e]), sy = dw_of2(p.shpdw[(size_t)(4 + i) * ne + e]),
+                 sz = dw_of2(p.shpdw[(size_t)(8 + i) * ne + e]);
         t[i][0] = dw_dot3c(sv[0], sx, sv[3], sy, sv[4], sz);
         t[i][1] = dw_dot3c(sv[3], sx, sv[1], sy, sv[5], sz);
         t[i][2] = dw_dot3c(sv[4], sx, sv[5], sy, sv[2], sz);
@@ -682,47 +682,31 @@ __global__ void __launch_bounds__(TPB) k_coordinate(KP p)
 // element geometry: volume_old swap, compute_volume, compute_shape_fn,
 // rotate_stress, compute_dt element terms
 // ==================================================================
-// a * b - c * d; in the mixed step's form (C) with one fused multiply-add
-template <bool C>
-__device__ __forceinline__ double cof(double a, double b, double c, double d)
-{
-    return C ? fma(a, b, -(c * d)) : a * b - c * d;
-}
-
-// FAST_RECIP: the mixed step's form, 1/(6 vol) by recip_newton, the
-// cofactors with fused multiply-adds (an ulp from the FP64 step's values),
-// and the first node's derivatives as minus the sum of the other three
-// (the four sum to zero: the element's nodal forces then balance)
-template <int ND, bool FAST_RECIP = false>
+// compute_shape_fn (geometry.cxx:368-455) of the FP64 step
+template <int ND>
 __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], const TetEdges &te, double vol,
                                               double (*shp)[ND + 1])
 {
     if (ND == 3) {
-        double iv = FAST_RECIP ? recip_newton(6 * vol) : 1 / (6 * vol);
+        double iv = 1 / (6 * vol);
         const double x01 = te.x01, x02 = te.x02, x03 = te.x03, x12 = te.x12, x13 = te.x13, x23 = te.x23;
         const double y01 = te.y01, y02 = te.y02, y03 = te.y03, y12 = te.y12, y13 = te.y13, y23 = te.y23;
         const double z01 = te.z01, z02 = te.z02, z03 = te.z03, z12 = te.z12, z13 = te.z13, z23 = te.z23;
-        if (!FAST_RECIP) {
-            shp[0][0] = iv * cof<FAST_RECIP>(y13, z12, y12, z13);
-            shp[1][0] = iv * cof<FAST_RECIP>(z13, x12, z12, x13);
-            shp[ND - 1][0] = iv * cof<FAST_RECIP>(x13, y12, x12, y13);
-        }
-        shp[0][1] = iv * cof<FAST_RECIP>(y02, z23, y23, z02);
-        shp[0][2] = iv * cof<FAST_RECIP>(y13, z03, y03, z13);
-        shp[0][3] = iv * cof<FAST_RECIP>(y01, z02, y02, z01);
-        shp[1][1] = iv * cof<FAST_RECIP>(z02, x23, z23, x02);
-        shp[1][2] = iv * cof<FAST_RECIP>(z13, x03, z03, x13);
-        shp[1][3] = iv * cof<FAST_RECIP>(z01, x02, z02, x01);
-        shp[ND - 1][1] = iv * cof<FAST_RECIP>(x02, y23, x23, y02);
-        shp[ND - 1][2] = iv * cof<FAST_RECIP>(x13, y03, x03, y13);
-        shp[ND - 1][3] = iv * cof<FAST_RECIP>(x01, y02, x02, y01);
-        if (FAST_RECIP) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) shp[k][0] = -((shp[k][1] + shp[k][2]) + shp[k][3]);
-        }
+        shp[0][0] = iv * (y13 * z12 - y12 * z13);
+        shp[1][0] = iv * (z13 * x12 - z12 * x13);
+        shp[ND - 1][0] = iv * (x13 * y12 - x12 * y13);
+        shp[0][1] = iv * (y02 * z23 - y23 * z02);
+        shp[0][2] = iv * (y13 * z03 - y03 * z13);
+        shp[0][3] = iv * (y01 * z02 - y02 * z01);
+        shp[1][1] = iv * (z02 * x23 - z23 * x02);
+        shp[1][2] = iv * (z13 * x03 - z03 * x13);
+        shp[1][3] = iv * (z01 * x02 - z02 * x01);
+        shp[ND - 1][1] = iv * (x02 * y23 - x23 * y02);
+        shp[ND - 1][2] = iv * (x13 * y03 - x03 * y13);
+        shp[ND - 1][3] = iv * (x01 * y02 - x02 * y01);
     } else {
         const double *d0 = d[0], *d1 = d[1], *d2 = d[2];
-        double iv = FAST_RECIP ? recip_newton(2 * vol) : 1 / (2 * vol);
+        double iv = 1 / (2 * vol);
         shp[0][0] = iv * (d1[1] - d2[1]);
         shp[0][1] = iv * (d2[1] - d0[1]);
         shp[0][2] = iv * (d0[1] - d1[1]);
@@ -735,10 +719,10 @@ __device__ __forceinline__ void shape_fn_elem(const double (*d)[ND], const TetEd
 // The mixed context's tet geometry from the edges at node 0, d_i = x_i - x_0
 // (9 FP64 differences instead of the reference formulas' 18): with the cross
 // products c1 = d2 x d3, c2 = d3 x d1, c3 = d1 x d2, the signed volume is
-// d1 . c1 / 6 (geometry.cxx:29-49 evaluates the same determinant from other
-// edges), dN_i/dx = c_i / (6 vol) for i = 1..3 and dN_0/dx = -(sum of the
-// other three), an ulp or so from compute_shape_fn's values
-// (geometry.cxx:368-455).  The determinant and every product stay FP64.
+// d1 . c1 / 6 in FP64 (geometry.cxx:29-49 evaluates the same determinant from
+// other edges), dN_i/dx = c_i / (6 vol) for i = 1..3 and dN_0/dx = -(sum of
+// the other three) (geometry.cxx:368-455), the latter in double-word
+// arithmetic (rel_shape_fn_dw).
 struct RelEdges {
     double d[3][3];   // d[i - 1][k]: component k of x_i - x_0
 };
@@ -763,25 +747,34 @@ __device__ __forceinline__ void cross3(const double *a, const double *b, double 
     out[2] = fma(a[0], b[1], -(a[1] * b[0]));
 }
 
-__device__ __forceinline__ double rel_volume(const RelEdges &r)
+// The mixed context's shape functions as double-word pairs: with the FP64
+// edges d_i and the volume's FP64 cross product c1 = d2 x d3, the cross
+// products c2 = d3 x d1 and c3 = d1 x d2 (compensated, dw_diff2), 1/(6 vol)
+// (dw_recip) and dN_i/dx = c_i / (6 vol), dN_0/dx = -(the other three),
+// all on the FP32 pipe; within ~2^-45 of the exact values where the FP64
+// forms carry one rounding per product.
+__device__ __forceinline__ void rel_shape_fn_dw(const RelEdges &r, const double *c1, double vol, dw (*shp)[4])
 {
-    double c1[3];
-    cross3(r.d[1], r.d[2], c1);
-    return div6(fma(r.d[0][2], c1[2], fma(r.d[0][1], c1[1], r.d[0][0] * c1[0])));
-}
-
-__device__ __forceinline__ void rel_shape_fn(const RelEdges &r, double vol, double (*shp)[4])
-{
-    double cc[3][3];
-    cross3(r.d[1], r.d[2], cc[0]);
-    cross3(r.d[2], r.d[0], cc[1]);
-    cross3(r.d[0], r.d[1], cc[2]);
-    const double iv = recip_newton(6 * vol);
+    dw d[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) d[i][k] = dw_split(r.d[i][k]);
+    dw cc[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) cc[0][k] = dw_split(c1[k]);
+    cc[1][0] = dw_diff2(d[2][1], d[0][2], d[2][2], d[0][1]);
+    cc[1][1] = dw_diff2(d[2][2], d[0][0], d[2][0], d[0][2]);
+    cc[1][2] = dw_diff2(d[2][0], d[0][1], d[2][1], d[0][0]);
+    cc[2][0] = dw_diff2(d[0][1], d[1][2], d[0][2], d[1][1]);
+    cc[2][1] = dw_diff2(d[0][2], d[1][0], d[0][0], d[1][2]);
+    cc[2][2] = dw_diff2(d[0][0], d[1][1], d[0][1], d[1][0]);
+    const dw iv = dw_recip(dw_mul(dw_split(vol), dw{6.0f, 0.0f}));
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
 #pragma unroll
-        for (int i = 1; i < 4; ++i) shp[k][i] = cc[i - 1][k] * iv;
-        shp[k][0] = -((shp[k][1] + shp[k][2]) + shp[k][3]);
+        for (int i = 1; i < 4; ++i) shp[k][i] = dw_mul(cc[i - 1][k], iv);
+        shp[k][0] = dw_neg(dw_sum3(shp[k][1], shp[k][2], shp[k][3]));
     }
 }
 
@@ -850,9 +843,12 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
         RelEdges re{};
         if (rel0 && (flags & (GEO_VOLUME | GEO_SHAPE))) re = rel_edges(c[0], c[1], c[2], c[NPE - 1]);
         else if (ND == 3 && (flags & (GEO_VOLUME | GEO_SHAPE))) te = tet_edges(c[0], c[1], c[2], c[NPE - 1]);
+        // the FP64 cross product d2 x d3 that the volume and the shape functions share
+        double c1[3] = {0, 0, 0};
+        if (rel0 && (flags & (GEO_VOLUME | GEO_SHAPE))) cross3(re.d[1], re.d[2], c1);
         if (flags & GEO_COPY_OLD) p.vol_old[e] = p.vol[e];
         if (flags & GEO_VOLUME) {
-            if (rel0) vol = rel_volume(re);
+            if (rel0) vol = div6(fma(re.d[0][2], c1[2], fma(re.d[0][1], c1[1], re.d[0][0] * c1[0])));
             else if (ND == 3) vol = tet_volume(te);
             else vol = tri_area<2>(c[0], c[1], c[2]);
             p.vol[e] = vol;
@@ -861,30 +857,43 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
             vol = p.vol[e];
         }
         double shp[ND][NPE];
+        float s32[ND][NPE];   // a mixed context's FP32 shape functions (its rotation's)
         if (flags & GEO_SHAPE) {
             if constexpr (ND == 3) {
-                if (rel0) rel_shape_fn(re, vol, shp);
-                else if (p.shp32) shape_fn_elem<ND, true>(c, te, vol, shp);
-                else shape_fn_elem<ND>(c, te, vol, shp);
-            } else if (p.shp32) shape_fn_elem<ND, true>(c, te, vol, shp);
-            else shape_fn_elem<ND>(c, te, vol, shp);
+                if (rel0) {   // the mixed context: double-word pairs and their FP32 high parts
+                    dw sdw[3][4];
+                    rel_shape_fn_dw(re, c1, vol, sdw);
 #pragma unroll
-            for (int k = 0; k < ND; ++k)
+                    for (int k = 0; k < 3; ++k)
 #pragma unroll
-                for (int i = 0; i < NPE; ++i) p.shp[((size_t)k * NPE + i) * ne + e] = shp[k][i];
-            if (p.shp32) {
+                        for (int i = 0; i < 4; ++i) {
+                            const size_t o = ((size_t)k * 4 + i) * ne + e;
+                            p.shpdw[o] = make_float2(sdw[k][i].hi, sdw[k][i].lo);
+                            p.shp32[o] = s32[k][i] = sdw[k][i].hi;
+                        }
+                } else {
+                    shape_fn_elem<ND>(c, te, vol, shp);
+                }
+            } else {
+                shape_fn_elem<ND>(c, te, vol, shp);
+            }
+            if (!rel0) {
 #pragma unroll
                 for (int k = 0; k < ND; ++k)
 #pragma unroll
-                    for (int i = 0; i < NPE; ++i) p.shp32[((size_t)k * NPE + i) * ne + e] = f32_of(shp[k][i]);
+                    for (int i = 0; i < NPE; ++i) p.shp[((size_t)k * NPE + i) * ne + e] = shp[k][i];
             }
         } else if (flags & GEO_ROTATE) {
 #pragma unroll
             for (int k = 0; k < ND; ++k)
 #pragma unroll
-                for (int i = 0; i < NPE; ++i) shp[k][i] = p.shp[((size_t)k * NPE + i) * ne + e];
+                for (int i = 0; i < NPE; ++i) {
+                    const size_t o = ((size_t)k * NPE + i) * ne + e;
+                    if (rel0) s32[k][i] = p.shp32[o];
+                    else shp[k][i] = p.shp[o];
+                }
         }
-        if ((flags & GEO_ROTATE) && ND == 3 && p.shp32) {
+        if ((flags & GEO_ROTATE) && rel0) {
             // mixed step: spin from FP32 velocity differences, FP32 Jaumann
             // increments added to the FP64 stress and strain.  Rounding the
             // velocities to FP32 moves a difference by ~2^-23 |v|: against
@@ -900,7 +909,7 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
                 double vi[ND];
                 load_node_v<ND>(p, nodes[i], vi);
                 const float d0 = f32_of(vi[0]) - v00, d1 = f32_of(vi[1]) - v01, d2 = f32_of(vi[ND - 1]) - v02;
-                const float sx = f32_of(shp[0][i]), sy = f32_of(shp[1][i]), sz = f32_of(shp[ND - 1][i]);
+                const float sx = s32[0][i], sy = s32[1][i], sz = s32[ND - 1][i];
                 w3 += 0.5f * (d0 * sy - d1 * sx);
                 w4 += 0.5f * (d0 * sz - d2 * sx);
                 w5 += 0.5f * (d1 * sz - d2 * sy);
@@ -1263,7 +1272,7 @@ __global__ void __launch_bounds__(TPB) k_rows(const __grid_constant__ RowTable t
             f.dev[soa] = v;
             if (f.dev32) f.dev32[soa] = f32_of(v);
         } else {
-            f.stage[aos] = f.dev[soa];
+            f.stage[aos] = f.dw ? f64_of(dw_of2(f.dw[soa])) : f.dev[soa];
         }
     }
 }
@@ -1470,6 +1479,21 @@ __global__ void k_f64_to_f32(const double *__restrict__ a, float *__restrict__ b
 int launch_f64_to_f32(const double *a, float *b, long long n, cudaStream_t s)
 {
     k_f64_to_f32<<<nblocks(n), TPB, 0, s>>>(a, b, n);
+    return 1;
+}
+
+// a mixed 3D context's shape functions: the double-word pairs -> FP64 (for downloads)
+__global__ void k_shp_join(const float2 *__restrict__ w, double *__restrict__ a, long long n)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) a[i] = f64_of(dw_of2(w[i]));
+}
+
+int launch_shp_join(const KP &p, cudaStream_t s)
+{
+    if (!p.shpdw) return 0;
+    const long long n = (long long)p.ne * p.npe * p.nd;
+    k_shp_join<<<nblocks(n), TPB, 0, s>>>(p.shpdw, p.shp, n);
     return 1;
 }
 

@@ -61,8 +61,11 @@ int launch_dt_reset(const KP &p, cudaStream_t s);
 // material constants: visc_coef[nmat], then 4 values per plastic table entry
 int launch_material_table(const KP &p, cudaStream_t s, double *out);
 
-// FP32 copy of an FP64 array (the mixed step's shape functions)
+// FP32 copy of an FP64 array
 int launch_f64_to_f32(const double *a, float *b, long long n, cudaStream_t s);
+// a mixed 3D context's shape functions (p.shpdw non-null; else no launch):
+// the double-word pairs -> FP64 p.shp, for a download
+int launch_shp_join(const KP &p, cudaStream_t s);
 
 // layout conversion between the reference's AoS rows and device SoA
 int launch_aos_to_soa(const double *aos, double *soa, int n, int ncomp, cudaStream_t s);
@@ -78,6 +81,7 @@ struct RowField {
     float *dev32;    // FP32 copy of dev, or null
     long long first; // index of the field's first value in the launch
     int n, nc, lo, hi;
+    const float2 *dw; // download: read the double-word pairs here instead of dev, or null
 };
 struct RowTable {
     RowField f[ROWS_MAX];

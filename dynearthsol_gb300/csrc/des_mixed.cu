@@ -26,6 +26,7 @@
 #include "des_kernels.cuh"
 #include "des_rheology.cuh"
 #include "des_mixed.cuh"
+#include "des_dw.cuh"
 
 namespace des {
 
@@ -437,21 +438,25 @@ __global__ void __launch_bounds__(TPB_M, 3) k_update_stress_mixed3(KP p, int fus
     if (bits) set_err(p, bits);
 }
 
-// strain rate (fields.cxx:166-232) from FP64 velocity differences.  Each
-// product dv_i,k * dN_i/dx_l is of the size of the whole row k of the
+// strain rate (fields.cxx:166-232) from the velocity differences to node 0.
+// Each product dv_i,k * dN_i/dx_l is of the size of the whole row k of the
 // velocity gradient, so an FP32 sum carries an absolute error ~eps32 |L|
 // into every component.  In the shear components that is harmless, but the
 // normal components set the volumetric rate, which the pressure integrates
 // with the bulk modulus (through the nodal-mixed dvoldt): in FP32 they alone
 // moved the stress by 1e-4 (relative L2) in 150 steps of a yielding case.
-// So the normal components are FP64 (FP64 shape functions), the shear ones
-// FP32.
+// So the normal components are double-word dot products (des_dw.cuh) of the
+// double-word velocity differences and shape functions, rounded to FP64
+// (~2^-45 of the row's terms), the shear ones FP32 from the pairs' high parts.
 __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, double *out)
 {
     const size_t ne = p.ne;
     double v0[3];
     load_node_v<3>(p, conn_at(p, 0, e), v0);
-    double dd[3][3];
+    dw w0[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) w0[d] = dw_neg(dw_split(v0[d]));
+    dw dd[3][3];
     float dv[3][3], sx[3], sy[3], sz[3];
 #pragma unroll
     for (int i = 1; i < 4; ++i) {
@@ -459,8 +464,8 @@ __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, doubl
         load_node_v<3>(p, conn_at(p, i, e), vi);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            dd[i - 1][d] = vi[d] - v0[d];
-            dv[i - 1][d] = f32_of(dd[i - 1][d]);
+            dd[i - 1][d] = dw_add(dw_split(vi[d]), w0[d]);
+            dv[i - 1][d] = dd[i - 1][d].hi;
         }
         sx[i - 1] = shp32_at(p, 0, i, e);
         sy[i - 1] = shp32_at(p, 1, i, e);
@@ -468,8 +473,8 @@ __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, doubl
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const double *h = p.shp + (size_t)k * 4 * ne + e;   // dN_i/dx_k at h[i * ne]
-        out[k] = fma(dd[2][k], h[3 * ne], fma(dd[1][k], h[2 * ne], dd[0][k] * h[ne]));
+        const float2 *h = p.shpdw + (size_t)k * 4 * ne + e;   // dN_i/dx_k at h[i * ne]
+        out[k] = f64_of(dw_dot3c(dd[0][k], dw_of2(h[ne]), dd[1][k], dw_of2(h[2 * ne]), dd[2][k], dw_of2(h[3 * ne])));
     }
     float s3 = 0, s4 = 0, s5 = 0;
 #pragma unroll

@@ -179,7 +179,11 @@ int des_device_status(des_ctx *ctx, unsigned *bits);
 /* Host <-> device state transfer (reference AoS layout <-> device SoA).
  * des_upload_state replaces the host->device re-upload after init, restart
  * and remesh (dynearthsol.cxx:80-99,179-215; remeshing.cxx:2009-2015);
- * des_download_state is called before host readers (output.cxx:79-208). */
+ * des_download_state is called before host readers (output.cxx:79-208).
+ * A DES_PREC_MIXED 3D context keeps its shape functions as double-word FP32
+ * pairs, formed from its coordinates and volumes: uploaded shape functions
+ * (here or by des_upload_fields) are not used, and downloads round the pairs
+ * to FP64. */
 int des_upload_state(des_ctx *ctx, const des_host_state *st);
 int des_download_state(des_ctx *ctx, des_host_state *st);
 
