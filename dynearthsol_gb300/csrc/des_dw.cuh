@@ -167,4 +167,27 @@ __device__ __forceinline__ dw dw_of2(float2 v) { return {v.x, v.y}; }
 // hi + lo rounded to FP64 (one FP64 addition; both conversions are exact)
 __device__ __forceinline__ double f64_of(dw x) { return f64_of(x.hi) + f64_of(x.lo); }
 
+// A running sum in Sum2's manner (Ogita, Rump, Oishi 2005): the high parts
+// summed with two_sum, the rounding errors and the low parts in the
+// compensation.  For the mixed step's node sums over a support list (a few
+// dozen terms): error at most ~n^2 u^2 of the terms' magnitudes, ~1e-12 in
+// the worst case, 1e-14 typically; 7 FP32 operations per FP32 term, 8 and a
+// split per FP64 term, against one FP64 addition.
+struct dw_sum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(dw x)
+    {
+        const dw t = two_sum(s, x.hi);
+        s = t.hi;
+        c += t.lo + x.lo;
+    }
+    __device__ __forceinline__ void add(float x)
+    {
+        const dw t = two_sum(s, x);
+        s = t.hi;
+        c += t.lo;
+    }
+    __device__ __forceinline__ double value() const { return f64_of(two_sum(s, c)); }
+};
+
 }  // namespace des

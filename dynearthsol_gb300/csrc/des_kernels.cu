@@ -305,6 +305,15 @@ __global__ void __launch_bounds__(TPB) k_nmd_gather(KP p)
 {
     int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= p.n_hi) return;
+    if (ND == 3 && p.shpdw) {   // a mixed context: double-word products, compensated FP32 sum (des_dw.cuh)
+        dw_sum acc;
+        for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+            const int e = p.sup_ent[q] >> 2;
+            acc.add(dw_mul(dw_split(p.dp[e]), dw_split(p.vol[e])));
+        }
+        p.ntmp[n] = acc.value() / p.vol_n[n];
+        return;
+    }
     double acc = 0;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
         int e = p.sup_ent[q] >> 2;
@@ -1067,7 +1076,9 @@ __global__ void __launch_bounds__(TPB) k_mass(KP p)
     if (n >= p.nn) return;
     const double pseudo_speed = p.prm.max_vbc_val * p.prm.inertial_scaling;
     const bool quasi = p.prm.is_quasi_static, thermal = p.prm.has_thermal_diffusion;
+    const bool cs = ND == 3 && p.shpdw;   // a mixed context: compensated FP32 sums, as k_mass_sum's
     double vn = 0, ms = 0, tm = 0;
+    dw_sum vs, mss, tms;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
         int e = p.sup_ent[q] >> 2;
         double vol = p.vol[e];
@@ -1075,9 +1086,21 @@ __global__ void __launch_bounds__(TPB) k_mass(KP p)
         double rho = quasi ? ((p.mat.nmat == 1) ? p.mat.rho_pseudo : m_bulkm(p, e) / (pseudo_speed * pseudo_speed))
                            : rho_e;
         double m = rho * vol / NPE;
-        vn += vol;
-        ms += m;
-        if (thermal) tm += rho_e * m_cp(p, e) * vol / NPE;
+        double tme = thermal ? rho_e * m_cp(p, e) * vol / NPE : 0.0;
+        if (cs) {
+            vs.add(dw_split(vol));
+            mss.add(dw_split(m));
+            if (thermal) tms.add(dw_split(tme));
+        } else {
+            vn += vol;
+            ms += m;
+            if (thermal) tm += tme;
+        }
+    }
+    if (cs) {
+        vn = vs.value();
+        ms = mss.value();
+        tm = tms.value();
     }
     p.vol_n[n] = vn;
     p.mass[n] = ms;
@@ -1092,6 +1115,19 @@ __global__ void __launch_bounds__(TPB) k_mass_sum(KP p)
     int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= p.n_hi) return;
     const bool thermal = p.prm.has_thermal_diffusion;
+    if (ND == 3 && p.shpdw) {   // a mixed context: compensated FP32 sums (des_dw.cuh), as k_mass's
+        dw_sum vs, mss, tms;
+        for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+            const int e = p.sup_ent[q] >> 2;
+            vs.add(dw_split(p.vol[e]));
+            mss.add(dw_split(p.me[e]));
+            if (thermal) tms.add(dw_split(p.tme[e]));
+        }
+        p.vol_n[n] = vs.value();
+        p.mass[n] = mss.value();
+        p.tmass[n] = thermal ? tms.value() : 0.0;
+        return;
+    }
     double vn = 0, ms = 0, tm = 0;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
         int e = p.sup_ent[q] >> 2;

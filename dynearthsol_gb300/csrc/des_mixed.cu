@@ -503,14 +503,16 @@ __global__ void __launch_bounds__(TPB_M) k_strain_rate_mixed3(KP p, int begin_st
 }
 
 // heat stencil on FP64 temperature differences (sum_j D_ij = 0), FP32
-// products, FP64 nodal sum; dvoldt in FP64 (fields.cxx:99-146, geometry.cxx:111-155)
+// products, a compensated FP32 nodal sum of the heat terms; dvoldt in FP64
+// (fields.cxx:99-146, geometry.cxx:111-155)
 __global__ void __launch_bounds__(TPB_M) k_heat_dvoldt_mixed3(KP p, int heat, int do_dvoldt)
 {
     int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= p.nn) return;
     const double Tn = p.T[n];
     const bool k_const = (p.mat.nmat == 1) && !p.ef[DES_EF_THERM_COND];
-    double tdot = 0, dvoldt = 0;
+    dw_sum tsum;   // a compensated FP32 sum of the heat terms (des_dw.cuh)
+    double dvoldt = 0;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
         const int ent = p.sup_ent[q];
         const int e = ent >> 2, i = ent & 3;
@@ -528,14 +530,14 @@ __global__ void __launch_bounds__(TPB_M) k_heat_dvoldt_mixed3(KP p, int heat, in
             const float volf = f32_of(vol);
             const float kv = f32_of(k_const ? p.mat.therm_cond[0] : m_k(p, e)) * volf;
             const float rh = f32_of((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * volf;
-            tdot += f64_of(kv * diffusion - rh);
+            tsum.add(kv * diffusion - rh);
         }
         if (do_dvoldt) {
             const double dj = p.srate[e] + p.srate[(size_t)p.ne + e] + p.srate[2 * (size_t)p.ne + e];
             dvoldt += dj * vol;
         }
     }
-    if (heat) p.tdot[n] = tdot;
+    if (heat) p.tdot[n] = tsum.value();
     if (do_dvoldt) p.ntmp[n] = dvoldt / p.vol_n[n];
 }
 
@@ -605,13 +607,20 @@ __global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat)
     int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= p.n_hi) return;
     const size_t ne = p.ne;
-    double tdot = 0, dvoldt = 0;
+    // the heat terms in a compensated FP32 sum (des_dw.cuh), as
+    // k_heat_dvoldt_mixed3 sums them; the dvoldt terms in FP64: they cancel
+    // between a node's elements, and the 2^-47 of a double-word split of
+    // each moved the volumetric rate enough to change the default damping's
+    // copysign at some nodes within ten steps
+    dw_sum tsum;
+    double dvoldt = 0;
     for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
         const int ent = p.sup_ent[q];
         const int e = ent >> 2, i = ent & 3;
-        if (heat) tdot += f64_of(p.hc[(size_t)i * ne + e]);
+        if (heat) tsum.add(p.hc[(size_t)i * ne + e]);
         dvoldt += p.qv[e];
     }
+    const double tdot = tsum.value();
     p.ntmp[n] = dvoldt / p.vol_n[n];
     if (heat) {   // temperature update + Dirichlet BC (fields.cxx:151-162)
         const unsigned flag = p.bcflag[n];
