@@ -86,9 +86,10 @@ __device__ __forceinline__ dw dw_dot3(dw a0, dw b0, dw a1, dw b1, dw a2, dw b2)
 // hi = x's sign, exponent and top 23 stored significand bits (x truncated to
 // 24 significant bits), lo = the remaining 29 bits, of x's sign, rounded to
 // float (2^23 + b - 2^23 gives the halves exactly, one fma joins them) and
-// scaled by a power of two.
-// |lo| < ulp(hi) and |x - (hi + lo)| <= 2^-47 |x|.  For |x| in [2^-126,
-// 2^128); smaller magnitudes give (0, 0), larger ones and NaN (inf / NaN, 0).
+// scaled by a power of two; then normalised by fast_two_sum.
+// |lo| <= ulp(hi) / 2 and |x - (hi + lo)| <= 2^-47 |x| for |x| in [2^-97, 2^128);
+// in [2^-126, 2^-97) lo is subnormal and the error below 2^-149 + 2^-47 |x|;
+// smaller magnitudes give (0, 0), larger ones and NaN (inf / NaN, 0).
 __device__ __forceinline__ dw dw_split(double x)
 {
     const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
@@ -108,7 +109,9 @@ __device__ __forceinline__ dw dw_split(double x)
         hb = (mag > 0x7ff00000u || (mag == 0x7ff00000u && lw)) ? 0x7fc00000u : 0x7f800000u;
         l = 0.0f;
     }
-    return {__uint_as_float(sg | hb), __uint_as_float(__float_as_uint(l) ^ sg)};
+    // normalised (exact): hi becomes the nearest float, |lo| <= ulp(hi) / 2,
+    // as the double-word algorithms' bounds assume of their operands
+    return fast_two_sum(__uint_as_float(sg | hb), __uint_as_float(__float_as_uint(l) ^ sg));
 }
 
 // a0 b0 + a1 b1 + a2 b2 for double-word operands: Dot2 on the high parts
@@ -141,7 +144,7 @@ __device__ __forceinline__ dw dw_sum3(dw x, dw y, dw z)
 
 // a b - c d for double-word operands (a cross-product component), in the
 // manner of dw_dot3c: exact high products and difference, the errors and the
-// cross terms in one float; error about 5u^2 (|a b| + |c d|)
+// cross terms in one float; error below 8u^2 (|a b| + |c d|)
 __device__ __forceinline__ dw dw_diff2(dw a, dw b, dw c, dw d)
 {
     const dw p = two_prod(a.hi, b.hi), q = two_prod(c.hi, d.hi);
@@ -153,7 +156,8 @@ __device__ __forceinline__ dw dw_diff2(dw a, dw b, dw c, dw d)
 // 1 / x for a double-word x of normal magnitude: the FP32 quotient r0 and one
 // Newton step r0 + r0 (1 - x r0), whose residual is formed exactly up to
 // x.lo r0 (x.hi r0 by two_prod, 1 - its high part exact as it lies within
-// 2u of 1); relative error about 3u^2
+// 2u of 1); relative error below 8u^2 (the residual's two roundings, the
+// correction's, and the step's quadratic term; tests/test_dw_arith.py)
 __device__ __forceinline__ dw dw_recip(dw x)
 {
     const float r0 = 1.0f / x.hi;
