@@ -396,14 +396,13 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     add((void **)&p.shp, (size_t)ne * npe * nd * D);
     // the mixed step's kernels are 3D; a plane-strain material runs the FP64 ones
     const bool mixed3 = (precision == DES_PREC_MIXED) && nd == 3 && !mat->is_plane_strain;
-    float *d_shp32 = nullptr, *d_hc = nullptr;
+    float *d_hc = nullptr;
     float4 *d_ft = nullptr;
     float2 *d_shpdw = nullptr;
     int *d_sup_pos = nullptr;
     double *d_qv = nullptr, *d_hc64 = nullptr;
     add((void **)&d_qv, (size_t)ne * D);
     if (mixed3) {
-        add((void **)&d_shp32, (size_t)ne * npe * nd * sizeof(float));
         add((void **)&d_hc, (size_t)ne * npe * sizeof(float));
         add((void **)&d_ft, (size_t)ne * npe * 2 * sizeof(float4));
         add((void **)&d_shpdw, (size_t)ne * npe * nd * sizeof(float2));
@@ -466,7 +465,6 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     p.rho_e = nullptr;
     p.buoy_e = nullptr;
     p.tdot = p.ntmp;
-    p.shp32 = d_shp32;
     p.shpdw = d_shpdw;
     p.hc = d_hc;
     p.qv = d_qv;
@@ -856,7 +854,7 @@ int des_upload_state(des_ctx *c, const des_host_state *st)
         return fail_msg(c->err, DES_EINPUT, "upload: coord, vel, temperature, volume_old, stress, strain and "
                         "plstrain are required");
     KP &p = c->kp;
-    const int nn = c->nn, ne = c->ne, nd = c->nd, npe = c->npe, nstr = c->nstr;
+    const int nn = c->nn, ne = c->ne, nd = c->nd, nstr = c->nstr;
     int rc;
     if ((rc = ensure_xfer(c))) return rc;
     // derived fields are taken from the host only when given as a set
@@ -1091,29 +1089,29 @@ int des_set_clock(des_ctx *c, double time, double dt, int steps)
     }
 
 PERFN(des_update_temperature,
-      n += (p.shp32 ? launch_heat_and_dvoldt_mixed(p, s, true, false) : launch_heat_gather(p, s));
+      n += (p.shpdw ? launch_heat_and_dvoldt_mixed(p, s, true, false) : launch_heat_gather(p, s));
       n += launch_temperature_update(p, s))
 PERFN(des_update_strain_rate,
-      n += (p.shp32 ? launch_strain_rate_mixed(p, s, false) : launch_strain_rate(p, s, false)))
+      n += (p.shpdw ? launch_strain_rate_mixed(p, s, false) : launch_strain_rate(p, s, false)))
 PERFN(des_compute_dvoldt, n += launch_dvoldt(p, s))
 PERFN(des_compute_edvoldt, n += launch_edvoldt(p, s))
 PERFN(des_update_stress,
-      n += ((p.shp32 && !p.mat.is_plane_strain) ? launch_update_stress_mixed(p, s, false)
+      n += (p.shpdw ? launch_update_stress_mixed(p, s, false)
                                                  : launch_update_stress(p, s, false)))
 PERFN(des_NMD_stress, n += launch_nmd_gather(p, s); n += launch_nmd_correct(p, s, false))
 // in a mixed context, the fused-multiply-add forms of the mixed step
 PERFN(des_update_force,
       n += launch_facet_forces(p, s); n += launch_force_terms(p, s);
-      n += launch_force(p, s, false, p.shp32 && !p.mat.is_plane_strain))
-PERFN(des_update_velocity, n += launch_velocity(p, s, p.shp32 && !p.mat.is_plane_strain))
+      n += launch_force(p, s, false, p.shpdw != nullptr))
+PERFN(des_update_velocity, n += launch_velocity(p, s, p.shpdw != nullptr))
 PERFN(des_apply_vbcs, n += launch_vbcs(p, s))
-PERFN(des_update_coordinate, n += launch_coordinate(p, s, p.shp32 && !p.mat.is_plane_strain))
+PERFN(des_update_coordinate, n += launch_coordinate(p, s, p.shpdw != nullptr))
 PERFN(des_swap_volume, n += launch_geometry(p, s, GEO_COPY_OLD))
 PERFN(des_compute_volume, n += launch_geometry(p, s, GEO_VOLUME))
 PERFN(des_compute_mass, n += launch_mass(p, s))
 PERFN(des_compute_shape_fn, n += launch_geometry(p, s, GEO_SHAPE))
 PERFN(des_rotate_stress, n += launch_geometry(p, s, GEO_ROTATE))
-PERFN(des_update_mesh, n += launch_coordinate(p, s, p.shp32 && !p.mat.is_plane_strain);
+PERFN(des_update_mesh, n += launch_coordinate(p, s, p.shpdw != nullptr);
       n += launch_geometry(p, s, GEO_COPY_OLD | GEO_VOLUME); n += launch_mass(p, s);
       n += launch_geometry(p, s, GEO_SHAPE))
 
@@ -1206,7 +1204,7 @@ int des_bad_mesh_quality(des_ctx *c, const des_quality_params *qp, int *code, in
 // ---- the fused step ----
 namespace {
 
-bool use_mixed(const des_ctx *c) { return c->kp.shp32 != nullptr && !c->kp.mat.is_plane_strain; }
+bool use_mixed(const des_ctx *c) { return c->kp.shpdw != nullptr; }
 
 // `mid` (optional) is recorded once nmd_correct is done: the kernels after it
 // (force and motion, geometry and rotation, mass sums, dt) write only x, v, f,
@@ -1295,7 +1293,6 @@ namespace {
 struct SlabField {
     double *host;
     double *dev;
-    float *dev32;
     int ncomp;
     bool node, up, down;
     double *stage;
@@ -1316,7 +1313,6 @@ bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &o
     KP &p = c->kp;
     const int nd = c->nd, npe = c->npe, nstr = c->nstr, ne = c->ne;
     const size_t shp1 = (size_t)ne * npe;
-    float *s32 = use_mixed(c) ? p.shp32 : nullptr;
     const float2 *dw = p.shpdw;
     const bool ps = p.mat.is_plane_strain != 0;
     const bool qs = p.prm.is_quasi_static != 0;
@@ -1324,30 +1320,30 @@ bool slab_fields(des_ctx *c, const des_host_state *st, std::vector<SlabField> &o
     // dpressure, edvoldt and ntmp are written before they are read; coord0
     // and, outside plane strain, stressyy are never written)
     const SlabField all[] = {
-        {st->coord, p.x, nullptr, nd, true, true, true, nullptr},
-        {st->coord0, p.x0, nullptr, nd, true, true, false, nullptr},
-        {st->vel, p.v, nullptr, nd, true, true, true, nullptr},
-        {st->force, p.f, nullptr, nd, true, false, true, nullptr},
-        {st->temperature, p.T, nullptr, 1, true, true, true, nullptr},
-        {st->mass, p.mass, nullptr, 1, true, !qs, true, nullptr},
-        {st->tmass, p.tmass, nullptr, 1, true, true, true, nullptr},
-        {st->volume_n, p.vol_n, nullptr, 1, true, false, true, nullptr},
-        {st->ntmp, p.ntmp, nullptr, 1, true, false, true, nullptr},
-        {st->volume, p.vol, nullptr, 1, false, false, true, nullptr},
-        {st->volume_old, p.vol_old, nullptr, 1, false, true, true, nullptr},
-        {st->stress, p.stress, nullptr, nstr, false, true, true, nullptr},
-        {st->strain, p.strain, nullptr, nstr, false, true, true, nullptr},
-        {st->strain_rate, p.srate, nullptr, nstr, false, false, true, nullptr},
-        {st->plstrain, p.pls, nullptr, 1, false, true, true, nullptr},
-        {st->delta_plstrain, p.dpls, nullptr, 1, false, true, true, nullptr},
-        {st->stressyy, p.syy, nullptr, 1, false, true, ps, nullptr},
-        {st->dpressure, p.dp, nullptr, 1, false, false, true, nullptr},
-        {st->edvoldt, p.edvoldt, nullptr, 1, false, false, true, nullptr},
-        {st->shpdx, p.shp, s32, npe, false, false, true, nullptr, dw},
-        {nd == 3 ? st->shpdy : nullptr, p.shp + shp1, s32 ? s32 + shp1 : nullptr, npe, false, false, nd == 3, nullptr,
+        {st->coord, p.x, nd, true, true, true, nullptr},
+        {st->coord0, p.x0, nd, true, true, false, nullptr},
+        {st->vel, p.v, nd, true, true, true, nullptr},
+        {st->force, p.f, nd, true, false, true, nullptr},
+        {st->temperature, p.T, 1, true, true, true, nullptr},
+        {st->mass, p.mass, 1, true, !qs, true, nullptr},
+        {st->tmass, p.tmass, 1, true, true, true, nullptr},
+        {st->volume_n, p.vol_n, 1, true, false, true, nullptr},
+        {st->ntmp, p.ntmp, 1, true, false, true, nullptr},
+        {st->volume, p.vol, 1, false, false, true, nullptr},
+        {st->volume_old, p.vol_old, 1, false, true, true, nullptr},
+        {st->stress, p.stress, nstr, false, true, true, nullptr},
+        {st->strain, p.strain, nstr, false, true, true, nullptr},
+        {st->strain_rate, p.srate, nstr, false, false, true, nullptr},
+        {st->plstrain, p.pls, 1, false, true, true, nullptr},
+        {st->delta_plstrain, p.dpls, 1, false, true, true, nullptr},
+        {st->stressyy, p.syy, 1, false, true, ps, nullptr},
+        {st->dpressure, p.dp, 1, false, false, true, nullptr},
+        {st->edvoldt, p.edvoldt, 1, false, false, true, nullptr},
+        {st->shpdx, p.shp, npe, false, false, true, nullptr, dw},
+        {nd == 3 ? st->shpdy : nullptr, p.shp + shp1, npe, false, false, nd == 3, nullptr,
          dw ? dw + shp1 : nullptr},
-        {st->shpdz, p.shp + (size_t)(nd - 1) * shp1, s32 ? s32 + (size_t)(nd - 1) * shp1 : nullptr, npe, false, false, true,
-         nullptr, dw ? dw + (size_t)(nd - 1) * shp1 : nullptr},
+        {st->shpdz, p.shp + (size_t)(nd - 1) * shp1, npe, false, false, true, nullptr,
+         dw ? dw + (size_t)(nd - 1) * shp1 : nullptr},
     };
     out.clear();
     size_t off = 0;
@@ -1435,7 +1431,7 @@ int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec
             CKC(cudaMemcpyAsync((f.ncomp == 1 ? f.dev : f.stage) + o, f.host + o, bytes, cudaMemcpyHostToDevice, xs));
             if (f.ncomp > 1) {
                 RowField &r = t.f[t.count++];
-                r = {f.stage, f.dev, f.dev32, t.total, f.node ? c->nn : c->ne, f.ncomp, lo, hi};
+                r = {f.stage, f.dev, t.total, f.node ? c->nn : c->ne, f.ncomp, lo, hi, nullptr};
                 t.total += (long long)(hi - lo) * f.ncomp;
             }
         }
@@ -1500,7 +1496,7 @@ int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec
             const int lo = f.node ? c->slab_n[flo] : c->slab_e[flo], hi = f.node ? c->slab_n[fhi] : c->slab_e[fhi];
             if (hi <= lo) continue;
             RowField &r = t.f[t.count++];
-            r = {f.stage, f.dev, nullptr, t.total, f.node ? c->nn : c->ne, f.ncomp, lo, hi, f.dw};
+            r = {f.stage, f.dev, t.total, f.node ? c->nn : c->ne, f.ncomp, lo, hi, f.dw};
             t.total += (long long)(hi - lo) * f.ncomp;
         }
         n += launch_rows(t, false, ys);

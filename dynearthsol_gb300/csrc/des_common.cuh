@@ -101,10 +101,10 @@ struct KP {
     double *buoy_e;                      // per-element rho g / NPE of the step (scratch), or null
     double *tdot;                        // node scratch for the heat gather (ntmp outside the fused step)
     double *fv;                          // [nd][nbf] per-facet stress-BC force (scratch)
-    float *shp32;                        // FP32 copy of shp for the mixed step, or null
-    // mixed 3D step: the shape functions as double-word pairs (hi, lo) at
-    // shp's indices, or null.  The mixed geometry writes these and shp32 (the
-    // pairs' hi parts) but not shp, which downloads fill from them on demand.
+    // mixed 3D step (a mixed context is one with shpdw): the shape functions
+    // as double-word pairs (hi, lo) at shp's indices, or null.  The hi parts
+    // are the FP32 shape functions.  The mixed geometry writes these but not
+    // shp, which downloads fill from them on demand.
     float2 *shpdw;
     float *hc;                           // [4][ne] per-element heat terms of the mixed step, or null
     double *qv;                          // [ne] per-element dvoldt term of the fused steps, or null

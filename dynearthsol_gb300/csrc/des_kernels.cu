@@ -848,7 +848,7 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
         double vol;
         TetEdges te{};
         // a mixed context's 3D geometry works from the edges at node 0
-        const bool rel0 = ND == 3 && p.shp32 != nullptr;
+        const bool rel0 = ND == 3 && p.shpdw != nullptr;
         RelEdges re{};
         if (rel0 && (flags & (GEO_VOLUME | GEO_SHAPE))) re = rel_edges(c[0], c[1], c[2], c[NPE - 1]);
         else if (ND == 3 && (flags & (GEO_VOLUME | GEO_SHAPE))) te = tet_edges(c[0], c[1], c[2], c[NPE - 1]);
@@ -869,7 +869,7 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
         float s32[ND][NPE];   // a mixed context's FP32 shape functions (its rotation's)
         if (flags & GEO_SHAPE) {
             if constexpr (ND == 3) {
-                if (rel0) {   // the mixed context: double-word pairs and their FP32 high parts
+                if (rel0) {   // the mixed context: double-word pairs (their high parts are the FP32 values)
                     dw sdw[3][4];
                     rel_shape_fn_dw(re, c1, vol, sdw);
 #pragma unroll
@@ -878,7 +878,7 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
                         for (int i = 0; i < 4; ++i) {
                             const size_t o = ((size_t)k * 4 + i) * ne + e;
                             p.shpdw[o] = make_float2(sdw[k][i].hi, sdw[k][i].lo);
-                            p.shp32[o] = s32[k][i] = sdw[k][i].hi;
+                            s32[k][i] = sdw[k][i].hi;
                         }
                 } else {
                     shape_fn_elem<ND>(c, te, vol, shp);
@@ -898,7 +898,7 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
 #pragma unroll
                 for (int i = 0; i < NPE; ++i) {
                     const size_t o = ((size_t)k * NPE + i) * ne + e;
-                    if (rel0) s32[k][i] = p.shp32[o];
+                    if (rel0) s32[k][i] = p.shpdw[o].x;
                     else shp[k][i] = p.shp[o];
                 }
         }
@@ -1304,9 +1304,7 @@ __global__ void __launch_bounds__(TPB) k_rows(const __grid_constant__ RowTable t
         const long long r = f.lo + j / f.nc, c = j % f.nc;
         const size_t aos = (size_t)r * f.nc + c, soa = (size_t)c * f.n + r;
         if (UP) {
-            const double v = f.stage[aos];
-            f.dev[soa] = v;
-            if (f.dev32) f.dev32[soa] = f32_of(v);
+            f.dev[soa] = f.stage[aos];
         } else {
             f.stage[aos] = f.dw ? f64_of(dw_of2(f.dw[soa])) : f.dev[soa];
         }

@@ -72,13 +72,11 @@ int launch_aos_to_soa(const double *aos, double *soa, int n, int ncomp, cudaStre
 int launch_soa_to_aos(const double *soa, double *aos, int n, int ncomp, cudaStream_t s);
 
 // The same conversion for the rows [lo, hi) of several fields in one launch
-// (one slab of the pipelined host step).  With dev32, the SoA values are also
-// written as FP32 (f32_of, as the mixed geometry pass rounds them).
+// (one slab of the pipelined host step).
 constexpr int ROWS_MAX = 12;
 struct RowField {
     double *stage;   // AoS rows [n][nc]; rows lo..hi-1 are read (up) or written
     double *dev;     // SoA [nc][n]
-    float *dev32;    // FP32 copy of dev, or null
     long long first; // index of the field's first value in the launch
     int n, nc, lo, hi;
     const float2 *dw; // download: read the double-word pairs here instead of dev, or null

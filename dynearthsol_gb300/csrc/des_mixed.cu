@@ -34,7 +34,7 @@ constexpr int TPB_M = 256;
 
 __device__ __forceinline__ float shp32_at(const KP &p, int k, int i, int e)
 {
-    return p.shp32[((size_t)k * 4 + i) * p.ne + e];
+    return p.shpdw[((size_t)k * 4 + i) * p.ne + e].x;   // the pair's high part: the nearest float
 }
 
 static inline int nblocks_m(long long n)
@@ -457,6 +457,7 @@ __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, doubl
 #pragma unroll
     for (int d = 0; d < 3; ++d) w0[d] = dw_neg(dw_split(v0[d]));
     dw dd[3][3];
+    float2 h[3][3];   // dN_i/dx_k of slots 1..3 as double-word pairs
     float dv[3][3], sx[3], sy[3], sz[3];
 #pragma unroll
     for (int i = 1; i < 4; ++i) {
@@ -467,15 +468,16 @@ __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, doubl
             dd[i - 1][d] = dw_add(dw_split(vi[d]), w0[d]);
             dv[i - 1][d] = dd[i - 1][d].hi;
         }
-        sx[i - 1] = shp32_at(p, 0, i, e);
-        sy[i - 1] = shp32_at(p, 1, i, e);
-        sz[i - 1] = shp32_at(p, 2, i, e);
+        h[0][i - 1] = p.shpdw[(size_t)i * ne + e];
+        h[1][i - 1] = p.shpdw[(size_t)(4 + i) * ne + e];
+        h[2][i - 1] = p.shpdw[(size_t)(8 + i) * ne + e];
+        sx[i - 1] = h[0][i - 1].x;
+        sy[i - 1] = h[1][i - 1].x;
+        sz[i - 1] = h[2][i - 1].x;
     }
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float2 *h = p.shpdw + (size_t)k * 4 * ne + e;   // dN_i/dx_k at h[i * ne]
-        out[k] = f64_of(dw_dot3c(dd[0][k], dw_of2(h[ne]), dd[1][k], dw_of2(h[2 * ne]), dd[2][k], dw_of2(h[3 * ne])));
-    }
+    for (int k = 0; k < 3; ++k)
+        out[k] = f64_of(dw_dot3c(dd[0][k], dw_of2(h[k][0]), dd[1][k], dw_of2(h[k][1]), dd[2][k], dw_of2(h[k][2])));
     float s3 = 0, s4 = 0, s5 = 0;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
