@@ -17,10 +17,12 @@
 //     exact sum, cancellation included;
 //   * dw_mul: the same paper, Algorithm 12 (DWTimesDW3): relative error
 //     below 4u^2;
-//   * dw_dot3, dw_sum3: the compensated dot product and sum Dot2 / Sum2 of
-//     Ogita, Rump, Oishi, "Accurate sum and dot product", SIAM J. Sci.
-//     Comput. 26(6), 2005, on the high parts, with the low parts' terms
-//     added to the compensation.
+//   * dw_dot3c, dw_diff2, dw_sum3, dw_sum: the compensated dot product and
+//     sum Dot2 / Sum2 of Ogita, Rump, Oishi, "Accurate sum and dot product",
+//     SIAM J. Sci. Comput. 26(6), 2005, on the high parts, with the low
+//     parts' terms added to the compensation.
+// tests/test_dw_arith.py restates each in numpy and holds it to its bound
+// against exact rational arithmetic.
 // The library is compiled with --fmad=false: no multiply and add below is
 // contracted beyond the fmaf calls written out.
 #pragma once
@@ -74,12 +76,6 @@ __device__ __forceinline__ dw dw_mul(dw x, dw y)
 }
 
 __device__ __forceinline__ dw dw_neg(dw x) { return {-x.hi, -x.lo}; }
-
-// a0 b0 + a1 b1 + a2 b2, three products and two sums
-__device__ __forceinline__ dw dw_dot3(dw a0, dw b0, dw a1, dw b1, dw a2, dw b2)
-{
-    return dw_add(dw_add(dw_mul(a0, b0), dw_mul(a1, b1)), dw_mul(a2, b2));
-}
 
 // The double-word form of an FP64 value by truncation, without an FP64
 // instruction:
