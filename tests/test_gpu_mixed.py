@@ -153,3 +153,52 @@ def test_gpu_mixed_force_double_word_vs_fp64():
           f"the net force is {np.median(net):.1e} of sum|T| (median)")
     assert ratio.max() <= 2.0 ** -42, ratio.max()
     assert np.count_nonzero(fb != fa) > 0
+
+
+def test_gpu_mixed_shape_functions_download_and_upload():
+    """A mixed context keeps its shape functions as double-word pairs formed
+    from the coordinates: the download (the pairs rounded to FP64) is within
+    1e-14 of the FP64 context's compute_shape_fn values, and an upload of
+    other shape-function values does not change them (they are re-formed
+    from the uploaded coordinates)."""
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import initial_state, make_workload
+    from dynearthsol_gb300.solver import DeviceModel
+    wl = make_workload("c1_3d_evp", cells=(6, 5, 3))
+    st, cp = initial_state(wl)
+    f = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_FP64)
+    init = f.init_fields(st)
+    clk = f.clock()
+    m = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_MIXED)
+    m.upload({k: v.copy() for k, v in init.items()}, clk)
+    a = m.download()
+    for k in ("shpdx", "shpdy", "shpdz"):
+        e = np.abs(a[k] - init[k]).max() / np.abs(init[k]).max()
+        assert e <= 1e-14, (k, e)
+    bad = {k: v.copy() for k, v in init.items()}
+    for k in ("shpdx", "shpdy", "shpdz"):
+        bad[k] *= 1.5
+    m.upload(bad, clk)
+    b = m.download()
+    for k in ("shpdx", "shpdy", "shpdz"):
+        np.testing.assert_array_equal(b[k], a[k], err_msg=k)
+
+
+def test_gpu_mixed_plane_strain_runs_the_fp64_kernels():
+    """A plane-strain material in a mixed 3D context runs the FP64 kernels:
+    the same bits as an FP64 context."""
+    from dataclasses import replace
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import initial_state, make_workload
+    from dynearthsol_gb300.solver import DeviceModel
+    wl = make_workload("c1_3d_evp", cells=(6, 5, 3))
+    wl.mat = replace(wl.mat, is_plane_strain=True)
+    st, cp = initial_state(wl)
+    out = []
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        m = DeviceModel(wl, comp_pressure=cp, precision=prec)
+        m.init_fields({k: v.copy() for k, v in st.items()})
+        m.step(20)
+        out.append(m.download())
+    for k in ("coord", "vel", "stress", "strain", "temperature", "shpdx"):
+        np.testing.assert_array_equal(out[0][k], out[1][k], err_msg=k)
