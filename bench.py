@@ -169,6 +169,36 @@ def port_baseline(wl, st, cp, clock, nthreads, budget_s=12.0):
                       f"OpenMP x{nthreads} (two-colour element bands), {dt:.1f} s"}
 
 
+def reference_sensitivity(wl, init, clock, cp, nsteps, fp64_final):
+    """How far the reference's own algorithm moves, over the same steps from
+    the same state, when its libm results move by +-1 ulp: the oracle (the
+    CPU restatement, OpenMP) run twice, once as built and once with every
+    transcendental result moved by -1, 0 or +1 ulp (liboracle_pert.so, one
+    xorshift stream per thread).  With the default damping this sets the
+    scale of any two faithful implementations' difference, the mixed step's
+    against the FP64 step's included; the device FP64 step's distance from
+    the plain oracle is reported beside it."""
+    from oracle.oracle import Oracle, state_copy
+    nth = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    runs = []
+    used = nth
+    for seed in (None, 12345):
+        s = state_copy(init)
+        o = Oracle(wl, s, cp, nth, clock, perturb_seed=seed)
+        used = o.threads
+        if o.run(nsteps):
+            raise RuntimeError("oracle run failed")
+        runs.append(s["stress"])
+    plain, pert = runs
+
+    def l2(x, y):
+        return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+    return {"steps": nsteps, "oracle_vs_oracle_pm1ulp_stress_rel_l2": l2(pert, plain),
+            "fp64_device_vs_oracle_stress_rel_l2": l2(fp64_final["stress"], plain),
+            "sample": f"the oracle on {used} host threads, {time.perf_counter() - t0:.1f} s for both runs"}
+
+
 def reference_cpu():
     """The reference's own step compiled with OpenMP (oracle/_ref), or None
     where its sources are not staged."""
@@ -428,6 +458,7 @@ def main():
     ms, launches, clocks = timed_steps(m, stream, args.steps, args.warmup, dist, True, local)
     value = aggregate_value(ne * args.steps, ms / 1e3, world)
     compare = None
+    fp64_final = None
     if args.precision == "mixed" and not args.no_compare:
         ms64, _, _ = timed_steps(f64, stream, args.steps, args.warmup, dist)
         a, b = f64.download(), m.download()
@@ -443,6 +474,7 @@ def main():
                                      "mixed_error_gate, damping option 2"),
                    "steps_compared": args.warmup + args.steps,
                    "max_normalised_err_vs_fp64": maxn}
+        fp64_final = a
 
     # ---- the mixed step's stress-error gate, on the same mesh with the
     # continuous damping option 2 (with the default option 1 the reference's
@@ -526,6 +558,9 @@ def main():
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(wl, init, cp, clock0, os.cpu_count() or 1)
+            if fp64_final is not None:   # beside the mixed-vs-FP64 figure it qualifies
+                line["cpu_baseline"]["reference_sensitivity"] = reference_sensitivity(
+                    wl, init, clock0, cp, args.warmup + args.steps, fp64_final)
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

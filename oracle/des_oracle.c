@@ -27,10 +27,30 @@
  * measure how far the reference's own algorithm drifts when its libm
  * differs in the last bit -- the envelope inside which any other faithful
  * implementation (another libm, another processor) must land. */
-static unsigned long long pert_state = 88172645463325252ull;
-void oracle_perturb_seed(unsigned long long s) { pert_state = s ? s : 88172645463325252ull; }
+/* One xorshift stream per thread: thread t starts from seed ^ (t * golden
+ * ratio) -- thread 0 from the seed itself -- whenever a new seed was set, so
+ * an OpenMP run (static schedule, fixed thread count) is reproducible and
+ * free of data races, and a one-thread run draws the single stream. */
+static unsigned long long pert_seed = 88172645463325252ull;
+static int pert_epoch = 1;
+static __thread unsigned long long pert_state;
+static __thread int pert_seen;
+void oracle_perturb_seed(unsigned long long s)
+{
+    pert_seed = s ? s : 88172645463325252ull;
+    ++pert_epoch;
+}
 static double pert_(double x)
 {
+    if (pert_seen != pert_epoch) {
+        int tid = 0;
+#ifdef _OPENMP
+        tid = omp_get_thread_num();
+#endif
+        pert_state = pert_seed ^ (0x9E3779B97F4A7C15ull * (unsigned long long)tid);
+        if (!pert_state) pert_state = 88172645463325252ull;
+        pert_seen = pert_epoch;
+    }
     pert_state ^= pert_state << 13;
     pert_state ^= pert_state >> 7;
     pert_state ^= pert_state << 17;
@@ -1559,6 +1579,28 @@ int oracle_boundary_normals(const des_mesh *mesh, const double *coord,
 /* ------------------------------------------------------------------ */
 /* context and driver                                                  */
 /* ------------------------------------------------------------------ */
+/* no node has elements in two bands of one colour (bands b and b' with
+ * |b - b'| >= 2) */
+static int bands_share_no_node(const des_mesh *mesh, const int *eg, int ng)
+{
+    const int nn = mesh->nnode, npe = mesh->ndims + 1;
+    int *lo = (int *)malloc(sizeof(int) * (size_t)nn), *hi = (int *)malloc(sizeof(int) * (size_t)nn);
+    for (int n = 0; n < nn; ++n) lo[n] = ng, hi[n] = -1;
+    for (int b = 0; b < ng; ++b)
+        for (int e = eg[b]; e < eg[b + 1]; ++e)
+            for (int i = 0; i < npe; ++i) {
+                const int n = mesh->connectivity[(size_t)e * npe + i];
+                if (b < lo[n]) lo[n] = b;
+                if (b > hi[n]) hi[n] = b;
+            }
+    int ok = 1;
+    for (int n = 0; n < nn && ok; ++n)
+        if (hi[n] - lo[n] >= 2) ok = 0;
+    free(lo);
+    free(hi);
+    return ok;
+}
+
 oracle_ctx *oracle_create(const des_mesh *mesh, const des_params *param, const des_material *mat,
                           int nthreads)
 {
@@ -1576,13 +1618,20 @@ oracle_ctx *oracle_create(const des_mesh *mesh, const des_params *param, const d
 #ifndef _OPENMP
     nthreads = 1;
 #endif
+    /* create_elem_groups (mesh.cxx:1724-1817): 2T contiguous bands, run as
+     * two colours.  Two bands of one colour must share no node, or the
+     * element scatters race: a node whose elements lie in bands two or more
+     * apart breaks that, and then the thread count is halved (down to one). */
+    c->egroups = (int *)malloc(sizeof(int) * (2 * (size_t)nthreads + 1));
+    for (;;) {
+        c->ngroups = nthreads > 1 ? 2 * nthreads : 1;
+        int per = c->ne / c->ngroups;
+        for (int i = 0; i < c->ngroups; i++) c->egroups[i] = i * per;
+        c->egroups[c->ngroups] = c->ne;
+        if (nthreads == 1 || bands_share_no_node(mesh, c->egroups, c->ngroups)) break;
+        nthreads /= 2;
+    }
     c->nthreads = nthreads;
-    /* create_elem_groups (mesh.cxx:1724-1817): 2T contiguous bands */
-    c->ngroups = nthreads > 1 ? 2 * nthreads : 1;
-    c->egroups = (int *)malloc(sizeof(int) * (c->ngroups + 1));
-    int per = c->ne / c->ngroups;
-    for (int i = 0; i < c->ngroups; i++) c->egroups[i] = i * per;
-    c->egroups[c->ngroups] = c->ne;
     c->tmp_nn = (double *)calloc((size_t)c->nn, sizeof(double));
     return c;
 }

@@ -93,6 +93,7 @@ class Oracle:
         L.oracle_bind_state.argtypes = [C.c_void_p, C.POINTER(capi.DesHostState)]
         L.oracle_set_elem_field.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
         L.oracle_run.argtypes = [C.c_void_p, C.c_int]
+        L.oracle_threads.argtypes = [C.c_void_p]
         L.oracle_init_fields.argtypes = [C.c_void_p]
         L.oracle_update_stress.argtypes = [C.c_void_p]
         L.oracle_compute_dt.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
@@ -128,6 +129,12 @@ class Oracle:
 
     def run(self, nsteps: int) -> int:
         return self.lib.oracle_run(self.ctx, nsteps)
+
+    @property
+    def threads(self) -> int:
+        """Threads the element loops use (fewer than asked where the
+        two-colour bands would share nodes)."""
+        return self.lib.oracle_threads(self.ctx)
 
     def call(self, name: str):
         if name == "update_stress":
