@@ -80,6 +80,12 @@ void invalidate_graph(des_ctx *c)
         cudaGraphExecDestroy(c->step_exec_mid);
         c->step_exec_mid = nullptr;
     }
+    for (cudaGraphExec_t &g : c->chain_exec) {
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    }
     if (c->pipe_exec) {
         cudaGraphExecDestroy(c->pipe_exec);
         c->pipe_exec = nullptr;
@@ -1236,6 +1242,39 @@ int enqueue_step_mixed(des_ctx *c, cudaEvent_t mid)
     return n;
 }
 
+// The chained mixed step (part 0 first, 1 middle, 2 last of des_step(n),
+// n >= 2).  update_mesh's passes end each step but the last as one
+// look-ahead pass that also does the next step's element pass (strain rate,
+// dvoldt and heat terms: the next step reads the same velocities, shape
+// functions, volumes and temperatures), and the next step's node pass forms
+// the mass sums before its own (nothing in between reads mass, tmass or
+// volume_n).  Every kernel does the arithmetic of enqueue_step_mixed's, so
+// n chained steps give the bits of n single steps; the last step ends as a
+// single step does, leaving the same state.
+int enqueue_step_mixed_chain(des_ctx *c, int part)
+{
+    const KP p = step_kp(c);
+    cudaStream_t s = c->stream;
+    int n = 0;
+    const bool thermal = p.prm.has_thermal_diffusion != 0;
+    if (part == 0) n += launch_elem_pass_mixed(p, s, thermal);
+    n += launch_node_pass_mixed(p, s, thermal, part != 0, part != 0);
+    n += launch_update_stress_mixed(p, s, true);
+    n += launch_nmd_gather(p, s);
+    n += launch_nmd_correct(p, s, true);
+    n += launch_force(p, s, true, true);
+    int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP | GEO_MASS_TERMS;
+    if (p.mat.rheol_type & DES_RH_ELASTIC) geo |= GEO_ROTATE;
+    if (part == 2) {
+        n += launch_geometry(p, s, geo);
+        n += launch_mass_sum(p, s);
+    } else {
+        n += launch_geometry_ahead(p, s, geo);
+    }
+    n += launch_dt_finalize(p, s, true);
+    return n;
+}
+
 int enqueue_step(des_ctx *c, cudaEvent_t mid)
 {
     if (use_mixed(c)) return enqueue_step_mixed(c, mid);
@@ -1279,6 +1318,23 @@ int build_step_graph(des_ctx *c, cudaEvent_t mid = nullptr)
         return cuda_fail(c, e, "cudaGraphInstantiate");
     }
     c->step_kernels = n;
+    return DES_OK;
+}
+
+int build_chain_graph(des_ctx *c, int part)
+{
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int n = enqueue_step_mixed_chain(c, part);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&c->chain_exec[part], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->chain_exec[part] = nullptr;
+        return cuda_fail(c, e, "cudaGraphInstantiate");
+    }
+    c->chain_kernels[part] = n;
     return DES_OK;
 }
 
@@ -1582,6 +1638,18 @@ int des_step(des_ctx *c, int nsteps)
 {
     if (!c || nsteps < 0) return DES_EINPUT;
     if (!c->has_state) return fail_msg(c->err, DES_EINPUT, "des_step before des_upload_state");
+    if (nsteps >= 2 && use_mixed(c)) {   // the chained step
+        for (int part = 0; part < 3; ++part) {
+            int rc;
+            if (!c->chain_exec[part] && (rc = build_chain_graph(c, part))) return rc;
+        }
+        for (int i = 0; i < nsteps; ++i) {
+            const int part = i == 0 ? 0 : (i == nsteps - 1 ? 2 : 1);
+            CK(cudaGraphLaunch(c->chain_exec[part], c->stream));
+            c->launches += c->chain_kernels[part];
+        }
+        return DES_OK;
+    }
     if (!c->step_exec) {
         int rc = build_step_graph(c);
         if (rc) return rc;

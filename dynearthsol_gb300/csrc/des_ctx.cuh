@@ -33,6 +33,11 @@ struct des_ctx {
     unsigned long long *d_red = nullptr;
     double *d_ef[DES_EF_COUNT] = {};
     cudaGraphExec_t step_exec = nullptr;
+    // the chained mixed step of des_step(n >= 2): its first, middle and last
+    // steps (a look-ahead geometry pass does the next step's element pass,
+    // and the next node pass the mass sums; the last step ends as one step)
+    cudaGraphExec_t chain_exec[3] = {};
+    int chain_kernels[3] = {};
     // pipelined host transfers, created by the first state transfer
     cudaStream_t xstream = nullptr;   // DMA between host rows and the device
     cudaEvent_t xev[DES_XFER_EVENTS] = {};

@@ -14,6 +14,7 @@
 #include "des_rheology.cuh"
 #include "des_bc.cuh"
 #include "des_dw.cuh"
+#include "des_mixed_elem.cuh"
 
 namespace des {
 
@@ -822,11 +823,14 @@ __device__ __forceinline__ void warp_block_min(unsigned long long val, unsigned 
     if ((threadIdx.x & 31) == 0) atomicMin(target, val);
 }
 
-// three blocks of 256 per SM (80 registers, ~150 bytes of spills to L1):
-// 24 warps hide the node gathers' latency better than 16 with 128 registers
-// (mixed step at 998,400 tets: 23 us less per step)
-template <int ND>
-__global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
+// The element geometry pass.  AHEAD (3D mixed contexts, the chained step's
+// look-ahead): with the shape-function pairs and the velocities still in
+// registers, it also does the next step's element pass (strain rate, dvoldt
+// and heat terms) -- the next step reads the same velocities, shape
+// functions, volume and temperature, none of which changes in between -- so
+// the pairs are not read back and one pass over the elements is saved.
+template <int ND, bool AHEAD>
+__device__ __forceinline__ void geometry_body(const KP &p, int flags)
 {
     constexpr int NSTR = ND * (ND + 1) / 2;
     constexpr int NPE = ND + 1;
@@ -865,12 +869,42 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
         } else {
             vol = p.vol[e];
         }
+        if (do_dt) {
+            // compute_dt element terms (geometry.cxx:254-292), while the coordinates are at hand
+            double minh;
+            if (ND == 3) {
+                // the largest face area: sqrt is correctly rounded and
+                // monotonic and /2 exact, so max_i sqrt(s_i) / 2 equals
+                // sqrt(max_i s_i) / 2 -- one square root instead of four
+                const double s2 = dmax_(dmax_(tri_area2_3d(c[0], c[1], c[2]), tri_area2_3d(c[0], c[1], c[NPE - 1])),
+                                        dmax_(tri_area2_3d(c[2], c[NPE - 1], c[0]),
+                                              tri_area2_3d(c[2], c[NPE - 1], c[1])));
+                double maxa = sqrt(s2) / 2;
+                minh = 3 * vol / maxa;
+            } else {
+                double d01 = 0, d12 = 0, d02 = 0;
+#pragma unroll
+                for (int k = 0; k < ND; ++k) {
+                    double a = c[1][k] - c[0][k], b = c[2][k] - c[1][k], cc = c[2][k] - c[0][k];
+                    d01 += a * a;
+                    d12 += b * b;
+                    d02 += cc * cc;
+                }
+                double maxl = sqrt(dmax_(dmax_(d01, d12), d02));
+                minh = 2 * vol / maxl;
+            }
+            b_minh = dbits(minh);
+            // uniform, the Maxwell time is formed once by k_dt_finalize
+            if (!uniform_maxwell_time(p)) b_maxwell = dbits(0.5 * p.mat.visc_min / (1e-40 + m_shearm(p, e)));
+            // the diffusion time 0.5 minh^2 / kappa is non-decreasing in minh,
+            // so its minimum over the elements is k_dt_finalize's 0.5 min(minh)^2 / kappa
+        }
         double shp[ND][NPE];
         float s32[ND][NPE];   // a mixed context's FP32 shape functions (its rotation's)
+        dw sdw[3][4];         // a mixed context's shape-function pairs
         if (flags & GEO_SHAPE) {
             if constexpr (ND == 3) {
                 if (rel0) {   // the mixed context: double-word pairs (their high parts are the FP32 values)
-                    dw sdw[3][4];
                     rel_shape_fn_dw(re, c1, vol, sdw);
 #pragma unroll
                     for (int k = 0; k < 3; ++k)
@@ -902,6 +936,12 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
                     else shp[k][i] = p.shp[o];
                 }
         }
+        double vv[NPE][ND];   // the nodes' velocities (a mixed context's rotation, the look-ahead)
+        float w3 = 0, w4 = 0, w5 = 0;   // a mixed context's spin
+        if (rel0 && ((flags & GEO_ROTATE) || AHEAD)) {
+#pragma unroll
+            for (int i = 0; i < NPE; ++i) load_node_v<ND>(p, nodes[i], vv[i]);
+        }
         if ((flags & GEO_ROTATE) && rel0) {
             // mixed step: spin from FP32 velocity differences, FP32 Jaumann
             // increments added to the FP64 stress and strain.  Rounding the
@@ -909,20 +949,31 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
             // differences ~|v| h / L across an element of size h in a field
             // varying over L, a relative error ~2^-23 L / h in the spin,
             // whose increment dt W s is itself ~1e-8 of the stress per step.
-            double v0[ND];
-            load_node_v<ND>(p, nodes[0], v0);
+            const double *v0 = vv[0];
             const float v00 = f32_of(v0[0]), v01 = f32_of(v0[1]), v02 = f32_of(v0[ND - 1]);
-            float w3 = 0, w4 = 0, w5 = 0;
 #pragma unroll
             for (int i = 1; i < NPE; ++i) {
-                double vi[ND];
-                load_node_v<ND>(p, nodes[i], vi);
+                const double *vi = vv[i];
                 const float d0 = f32_of(vi[0]) - v00, d1 = f32_of(vi[1]) - v01, d2 = f32_of(vi[ND - 1]) - v02;
                 const float sx = s32[0][i], sy = s32[1][i], sz = s32[ND - 1][i];
                 w3 += 0.5f * (d0 * sy - d1 * sx);
                 w4 += 0.5f * (d0 * sz - d2 * sx);
                 w5 += 0.5f * (d1 * sz - d2 * sy);
             }
+        }
+        if constexpr (AHEAD && ND == 3) {   // the next step's element pass (k_elem_pass_mixed3's arithmetic)
+            float2 h[3][3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int i = 1; i < 4; ++i) h[k][i - 1] = make_float2(sdw[k][i].hi, sdw[k][i].lo);
+            double sr[6];
+            strain_rate_mixed_vals(vv, h, sr);
+#pragma unroll
+            for (int cc = 0; cc < 6; ++cc) p.srate[cc * ne + e] = sr[cc];
+            elem_terms_mixed(p, e, sr, vol, s32, p.prm.has_thermal_diffusion != 0);
+        }
+        if ((flags & GEO_ROTATE) && rel0) {
             const float dtf = f32_of(p.clk->dt);
             double *arr[2] = {p.stress, p.strain};
 #pragma unroll
@@ -991,41 +1042,25 @@ __global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
             p.me[e] = rho * vol / NPE;
             if (p.prm.has_thermal_diffusion) p.tme[e] = rho_e * m_cp(p, e) * vol / NPE;
         }
-        if (do_dt) {
-            // compute_dt element terms (geometry.cxx:254-292)
-            double minh;
-            if (ND == 3) {
-                // the largest face area: sqrt is correctly rounded and
-                // monotonic and /2 exact, so max_i sqrt(s_i) / 2 equals
-                // sqrt(max_i s_i) / 2 -- one square root instead of four
-                const double s2 = dmax_(dmax_(tri_area2_3d(c[0], c[1], c[2]), tri_area2_3d(c[0], c[1], c[NPE - 1])),
-                                        dmax_(tri_area2_3d(c[2], c[NPE - 1], c[0]),
-                                              tri_area2_3d(c[2], c[NPE - 1], c[1])));
-                double maxa = sqrt(s2) / 2;
-                minh = 3 * vol / maxa;
-            } else {
-                double d01 = 0, d12 = 0, d02 = 0;
-#pragma unroll
-                for (int k = 0; k < ND; ++k) {
-                    double a = c[1][k] - c[0][k], b = c[2][k] - c[1][k], cc = c[2][k] - c[0][k];
-                    d01 += a * a;
-                    d12 += b * b;
-                    d02 += cc * cc;
-                }
-                double maxl = sqrt(dmax_(dmax_(d01, d12), d02));
-                minh = 2 * vol / maxl;
-            }
-            b_minh = dbits(minh);
-            // uniform, the Maxwell time is formed once by k_dt_finalize
-            if (!uniform_maxwell_time(p)) b_maxwell = dbits(0.5 * p.mat.visc_min / (1e-40 + m_shearm(p, e)));
-            // the diffusion time 0.5 minh^2 / kappa is non-decreasing in minh,
-            // so its minimum over the elements is k_dt_finalize's 0.5 min(minh)^2 / kappa
-        }
     }
     if (do_dt) {   // uniform across the grid: every thread reaches the shuffles
         warp_block_min<ND>(b_minh, &p.clk->red_minh);
         if (!uniform_maxwell_time(p)) warp_block_min<ND>(b_maxwell, &p.clk->red_maxwell);
     }
+}
+
+// three blocks of 256 per SM (80 registers, ~150 bytes of spills to L1):
+// 24 warps hide the node gathers' latency better than 16 with 128 registers
+// (mixed step at 998,400 tets: 23 us less per step)
+template <int ND>
+__global__ void __launch_bounds__(TPB, 3) k_geometry(KP p, int flags)
+{
+    geometry_body<ND, false>(p, flags);
+}
+
+__global__ void __launch_bounds__(TPB, 3) k_geometry_ahead3(KP p, int flags)
+{
+    geometry_body<3, true>(p, flags);
 }
 
 // compute_dt final combination (geometry.cxx:294-309), single thread
@@ -1456,6 +1491,12 @@ int launch_coordinate(const KP &p, cudaStream_t s, bool contract)
 int launch_geometry(const KP &p, cudaStream_t s, int flags)
 {
     DISPATCH(k_geometry, nblocks(p.e_hi - p.e_lo), p, flags);
+    return 1;
+}
+
+int launch_geometry_ahead(const KP &p, cudaStream_t s, int flags)
+{
+    k_geometry_ahead3<<<nblocks(p.e_hi - p.e_lo), TPB, 0, s>>>(p, flags);
     return 1;
 }
 

@@ -47,6 +47,9 @@ int launch_velocity(const KP &p, cudaStream_t s, bool contract = false);
 int launch_vbcs(const KP &p, cudaStream_t s);
 int launch_coordinate(const KP &p, cudaStream_t s, bool contract = false);
 int launch_geometry(const KP &p, cudaStream_t s, int flags);
+// the chained mixed step's geometry pass (3D mixed contexts), which also
+// does the next step's element pass (k_elem_pass_mixed3's work)
+int launch_geometry_ahead(const KP &p, cudaStream_t s, int flags);
 int launch_mass(const KP &p, cudaStream_t s);
 // compute_mass from the element terms of a GEO_MASS_TERMS geometry pass (same sums, same order)
 int launch_mass_sum(const KP &p, cudaStream_t s);

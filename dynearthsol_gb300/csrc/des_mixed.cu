@@ -27,6 +27,7 @@
 #include "des_rheology.cuh"
 #include "des_mixed.cuh"
 #include "des_dw.cuh"
+#include "des_mixed_elem.cuh"
 
 namespace des {
 
@@ -438,56 +439,20 @@ __global__ void __launch_bounds__(TPB_M, 3) k_update_stress_mixed3(KP p, int fus
     if (bits) set_err(p, bits);
 }
 
-// strain rate (fields.cxx:166-232) from the velocity differences to node 0.
-// Each product dv_i,k * dN_i/dx_l is of the size of the whole row k of the
-// velocity gradient, so an FP32 sum carries an absolute error ~eps32 |L|
-// into every component.  In the shear components that is harmless, but the
-// normal components set the volumetric rate, which the pressure integrates
-// with the bulk modulus (through the nodal-mixed dvoldt): in FP32 they alone
-// moved the stress by 1e-4 (relative L2) in 150 steps of a yielding case.
-// So the normal components are double-word dot products (des_dw.cuh) of the
-// double-word velocity differences and shape functions, rounded to FP64
-// (~2^-45 of the row's terms), the shear ones FP32 from the pairs' high parts.
+// strain rate (fields.cxx:166-232) of one element, loaded from memory and
+// formed by strain_rate_mixed_vals (des_mixed_elem.cuh)
 __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, double *out)
 {
     const size_t ne = p.ne;
-    double v0[3];
-    load_node_v<3>(p, conn_at(p, 0, e), v0);
-    dw w0[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) w0[d] = dw_neg(dw_split(v0[d]));
-    dw dd[3][3];
+    double v[4][3];
     float2 h[3][3];   // dN_i/dx_k of slots 1..3 as double-word pairs
-    float dv[3][3], sx[3], sy[3], sz[3];
 #pragma unroll
-    for (int i = 1; i < 4; ++i) {
-        double vi[3];
-        load_node_v<3>(p, conn_at(p, i, e), vi);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            dd[i - 1][d] = dw_add(dw_split(vi[d]), w0[d]);
-            dv[i - 1][d] = dd[i - 1][d].hi;
-        }
-        h[0][i - 1] = p.shpdw[(size_t)i * ne + e];
-        h[1][i - 1] = p.shpdw[(size_t)(4 + i) * ne + e];
-        h[2][i - 1] = p.shpdw[(size_t)(8 + i) * ne + e];
-        sx[i - 1] = h[0][i - 1].x;
-        sy[i - 1] = h[1][i - 1].x;
-        sz[i - 1] = h[2][i - 1].x;
-    }
+    for (int i = 0; i < 4; ++i) load_node_v<3>(p, conn_at(p, i, e), v[i]);
 #pragma unroll
     for (int k = 0; k < 3; ++k)
-        out[k] = f64_of(dw_dot3c(dd[0][k], dw_of2(h[k][0]), dd[1][k], dw_of2(h[k][1]), dd[2][k], dw_of2(h[k][2])));
-    float s3 = 0, s4 = 0, s5 = 0;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        s3 += 0.5f * (dv[i][0] * sy[i] + dv[i][1] * sx[i]);
-        s4 += 0.5f * (dv[i][0] * sz[i] + dv[i][2] * sx[i]);
-        s5 += 0.5f * (dv[i][1] * sz[i] + dv[i][2] * sy[i]);
-    }
-    out[3] = f64_of(s3);
-    out[4] = f64_of(s4);
-    out[5] = f64_of(s5);
+        for (int i = 1; i < 4; ++i) h[k][i - 1] = p.shpdw[((size_t)k * 4 + i) * ne + e];
+    strain_rate_mixed_vals(v, h, out);
 #pragma unroll
     for (int c = 0; c < 6; ++c) p.srate[c * ne + e] = out[c];
 }
@@ -563,52 +528,51 @@ __global__ void __launch_bounds__(TPB_M) k_elem_pass_mixed3(KP p, int heat)
         p.clk->time += p.clk->dt;
     }
     if (e >= p.e_hi) return;
-    const size_t ne = p.ne;
     double sr[6];
     strain_rate_mixed_elem(p, e, sr);
-    const double vol = p.vol[e];
-    p.qv[e] = (sr[0] + sr[1] + sr[2]) * vol;   // compute_dvoldt term (geometry.cxx:127-135)
-    if (!heat) return;
-    double T[4];
-    float sx[4], sy[4], sz[4];
+    float s32[3][4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        T[i] = p.T[conn_at(p, i, e)];
-        sx[i] = shp32_at(p, 0, i, e);
-        sy[i] = shp32_at(p, 1, i, e);
-        sz[i] = shp32_at(p, 2, i, e);
-    }
-    // D_ij = D_ji and f32_of(T_i - T_j) = -f32_of(T_j - T_i) bit for bit,
-    // so each of the six products serves both rows
-    float P[4][4];
+    for (int k = 0; k < 3; ++k)
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = i + 1; j < 4; ++j) {
-            const float D = sx[i] * sx[j] + sy[i] * sy[j] + sz[i] * sz[j];
-            const float t = D * f32_of(T[j] - T[i]);
-            P[i][j] = t;
-            P[j][i] = -t;
-        }
-    const bool k_const = (p.mat.nmat == 1) && !p.ef[DES_EF_THERM_COND];
-    const float volf = f32_of(vol);
-    const float kv = f32_of(k_const ? p.mat.therm_cond[0] : m_k(p, e)) * volf;
-    const float rh = f32_of((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * volf;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        float diffusion = 0.0f;
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (j != i) diffusion += P[i][j];
-        p.hc[(size_t)i * ne + e] = kv * diffusion - rh;
-    }
+        for (int i = 0; i < 4; ++i) s32[k][i] = shp32_at(p, k, i, e);
+    elem_terms_mixed(p, e, sr, p.vol[e], s32, heat);
 }
 
-__global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat)
+// The node pass: heat and dvoldt sums, the temperature update.  In the
+// chained step (mass_sums) it first forms the previous step's compute_mass
+// sums (volume_n, mass, tmass) from the element terms that its look-ahead
+// geometry pass wrote, as k_mass_sum forms them, and (begin_step) starts the
+// step's clock, which the look-ahead pass could not: the step's dt is final
+// only after k_dt_finalize.
+__global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat, int mass_sums, int begin_step)
 {
+    if (begin_step && blockIdx.x == 0 && threadIdx.x == 0) {   // dynearthsol.cxx:325-326
+        p.clk->steps += 1;
+        p.clk->time += p.clk->dt;
+    }
     int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= p.n_hi) return;
     const size_t ne = p.ne;
+    const int q0 = p.sup_off[n], q1 = p.sup_off[n + 1];
+    double vol_n, tmass = 0;
+    if (mass_sums) {   // compensated FP32 sums (des_dw.cuh), as k_mass_sum's
+        const bool thermal = p.prm.has_thermal_diffusion;
+        dw_sum vs, mss, tms;
+        for (int q = q0; q < q1; ++q) {
+            const int e = p.sup_ent[q] >> 2;
+            vs.add(dw_split(p.vol[e]));
+            mss.add(dw_split(p.me[e]));
+            if (thermal) tms.add(dw_split(p.tme[e]));
+        }
+        vol_n = vs.value();
+        tmass = thermal ? tms.value() : 0.0;
+        p.vol_n[n] = vol_n;
+        p.mass[n] = mss.value();
+        p.tmass[n] = tmass;
+    } else {
+        vol_n = p.vol_n[n];
+        if (heat) tmass = p.tmass[n];
+    }
     // the heat terms in a compensated FP32 sum (des_dw.cuh), as
     // k_heat_dvoldt_mixed3 sums them; the dvoldt terms in FP64: they cancel
     // between a node's elements, and the 2^-47 of a double-word split of
@@ -616,19 +580,19 @@ __global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat)
     // copysign at some nodes within ten steps
     dw_sum tsum;
     double dvoldt = 0;
-    for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
+    for (int q = q0; q < q1; ++q) {
         const int ent = p.sup_ent[q];
         const int e = ent >> 2, i = ent & 3;
         if (heat) tsum.add(p.hc[(size_t)i * ne + e]);
         dvoldt += p.qv[e];
     }
     const double tdot = tsum.value();
-    p.ntmp[n] = dvoldt / p.vol_n[n];
+    p.ntmp[n] = dvoldt / vol_n;
     if (heat) {   // temperature update + Dirichlet BC (fields.cxx:151-162)
         const unsigned flag = p.bcflag[n];
         if (flag & BOUNDZ1) p.T[n] = p.prm.surface_temperature;
         else if ((flag & BOUNDZ0) && !p.prm.has_fixed_bottom_temperature) p.T[n] = p.prm.mantle_temperature;
-        else p.T[n] -= tdot * p.clk->dt / p.tmass[n];
+        else p.T[n] -= tdot * p.clk->dt / tmass;
     }
 }
 
@@ -658,9 +622,9 @@ int launch_elem_pass_mixed(const KP &p, cudaStream_t s, bool heat)
     return 1;
 }
 
-int launch_node_pass_mixed(const KP &p, cudaStream_t s, bool heat)
+int launch_node_pass_mixed(const KP &p, cudaStream_t s, bool heat, bool mass_sums, bool begin_step)
 {
-    k_node_pass_mixed3<<<nblocks_m(p.n_hi - p.n_lo), TPB_M, 0, s>>>(p, (int)heat);
+    k_node_pass_mixed3<<<nblocks_m(p.n_hi - p.n_lo), TPB_M, 0, s>>>(p, (int)heat, (int)mass_sums, (int)begin_step);
     return 1;
 }
 

@@ -109,6 +109,62 @@ def test_gpu_mixed_fused_equals_function_sequence():
         np.testing.assert_array_equal(sa[k], sb[k], err_msg=k)
 
 
+def _chained_vs_single(wl, cp, init, clock, nsteps):
+    """nsteps as one des_step call (the chained step) and as nsteps calls of
+    one step, from the same state: every downloaded field and the clock
+    identical.  Returns the kernel launches of both."""
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.solver import DeviceModel
+    a = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_MIXED)
+    b = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_MIXED)
+    a.upload({k: v.copy() for k, v in init.items()}, clock)
+    b.upload({k: v.copy() for k, v in init.items()}, clock)
+    l0 = a.launches()
+    a.step(nsteps)
+    chained = a.launches() - l0
+    l0 = b.launches()
+    for _ in range(nsteps):
+        b.step(1)
+    single = b.launches() - l0
+    sa, sb = a.download(), b.download()
+    assert a.device_status() == 0 and b.device_status() == 0
+    for k in sa:
+        if sa[k] is not None:
+            np.testing.assert_array_equal(sa[k], sb[k], err_msg=k)
+    assert a.clock() == b.clock()
+    return chained, single
+
+
+def test_gpu_mixed_chained_steps_equal_single_steps():
+    """des_step(n >= 2) in a mixed context runs the chained step (a
+    look-ahead geometry pass that also does the next step's element pass,
+    the mass sums folded into the next node pass): its bits are those of n
+    single steps, for every field and the clock, over windows that start
+    and end off the tenth steps (where dt changes) -- with heat and several
+    materials, and in a yielding case."""
+    from cases import build_case
+    from conftest import load_golden, state_from
+    from dynearthsol_gb300 import capi
+    from dynearthsol_gb300.config import initial_state
+    from dynearthsol_gb300.solver import DeviceModel
+    g = load_golden("3d_heat_jitter_multimat")
+    wl, _ = build_case("3d_heat_jitter_multimat")
+    cp = float(g["init"]["compensation_pressure"])
+    c = g["init"]["clock"]
+    for n in (2, 3, 13):
+        chained, single = _chained_vs_single(wl, cp, state_from(g["init"]), (c[0], c[1], int(c[2])), n)
+        print(f"heat, several materials, {n} steps: {chained} launches chained, {single} single")
+        assert chained < single
+    wl, n = build_case("3d_evp_yield")
+    st, cp = initial_state(wl)
+    f = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_FP64)
+    init = f.init_fields(st)
+    clock = f.clock()
+    f.close()
+    chained, single = _chained_vs_single(wl, cp, init, clock, n)
+    print(f"yielding, {n} steps: {chained} launches chained, {single} single")
+
+
 def test_gpu_mixed_force_double_word_vs_fp64():
     """update_force in a mixed context (element terms T = (sigma . dN/dx +
     rho g / 4 z) vol in double-word FP32 arithmetic, summed per node in
