@@ -362,7 +362,10 @@ int des_set_clock(des_ctx *ctx, double time, double dt, int steps);
 /* Run nsteps explicit steps: the body of the reference's time loop
  * (dynearthsol.cxx:325-361) without phase changes, output and remeshing,
  * with compute_dt every 10th step on the device.  Uses the fused kernel
- * schedule; results equal the per-function sequence. */
+ * schedule; results equal the per-function sequence.  In a DES_PREC_MIXED
+ * context, nsteps >= 2 chains the steps (each geometry pass but the last
+ * also does the next step's element pass); the results are those of
+ * nsteps calls of one step, bit for bit. */
 int des_step(des_ctx *ctx, int nsteps);
 
 /* Same as des_step, but with the state in HOST memory in the reference's
