@@ -532,10 +532,16 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
         if (e1 == cudaSuccess) e1 = cudaStreamSynchronize(c->stream);
         if (e1 == cudaSuccess) {
             for (int m = 0; m < nm; ++m) p.mat.visc_coef[m] = tab[m];
-            p.mat.visc_lnc = std::log(0.25e6 * tab[0]);
+            p.mat.visc_skip_empty = 1;
+            for (int m = 0; m < nm; ++m) {
+                p.mat.visc_lnc[m] = std::log(0.25e6 * tab[m]);
+                p.mat.visc_qnr[m] = p.mat.visc_activation_energy[m] / (p.mat.visc_exponent[m] * 8.3144);
+                if (!(tab[m] > 0 && std::isfinite(tab[m]) && p.mat.visc_activation_energy[m] >= 0
+                      && p.mat.visc_exponent[m] > 0))
+                    p.mat.visc_skip_empty = 0;
+            }
             p.mat.visc_lnmin = std::log(p.mat.visc_min);
             p.mat.visc_lnmax = std::log(p.mat.visc_max);
-            p.mat.visc_qnr = p.mat.visc_activation_energy[0] / (p.mat.visc_exponent[0] * 8.3144);
             for (int k = 0; k < 2 * nm; ++k) {
                 p.mat.pt_anphi[k] = tab[nm + 4 * k + 0];
                 p.mat.pt_anpsi[k] = tab[nm + 4 * k + 1];

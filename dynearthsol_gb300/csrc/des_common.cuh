@@ -63,9 +63,13 @@ struct MatC {
     double visc_pw1[DES_MAXMAT];     // -1 / n                  (matprops.cxx:299)
     double visc_coef[DES_MAXMAT];    // pow(0.75 * A, -1 / n)   (matprops.cxx:300)
     double rho_pseudo;               // bulkm / (v_max * inertial_scaling)^2 (geometry.cxx:348-349), nmat == 1
-    double visc_lnc;                 // ln(0.25e6 * visc_coef[0])   (mixed step, nmat == 1)
+    double visc_lnc[DES_MAXMAT];     // ln(0.25e6 * visc_coef[m])   (mixed step)
     double visc_lnmin, visc_lnmax;   // ln(visc_min), ln(visc_max)  (mixed step)
-    double visc_qnr;                 // Q / (n R)                   (mixed step)
+    double visc_qnr[DES_MAXMAT];     // Q / (n R)                   (mixed step)
+    // every material's viscosity law is positive wherever T > 0 (A > 0, Q >= 0,
+    // n > 0), so a material without markers in the element adds exactly +0
+    // to the harmonic sum of MatProps::visc and can be skipped
+    int visc_skip_empty;
     double hr_over_cp;               // hr / cp (fields.cxx:118), nmat == 1
     // plastic_props at the material's start / saturated angles
     // (matprops.cxx:365-372): entry 2m at (phi0, psi0), 2m+1 at (phi1, psi1)
@@ -348,11 +352,13 @@ __device__ double m_visc(const KP &p, int e, const double *edot)
         ed = dmax_(ed, min_strain_rate);
         double result = 0;
         int n = 0;
+        const bool skip_empty = p.mat.visc_skip_empty && T > 0;
         for (int m = 0; m < p.mat.nmat; m++) {
+            int k = mcount(p, e, m);
+            if (k == 0 && skip_empty) continue;   // k / visc0 = +0 exactly
             const double pw = p.mat.visc_pw[m];
             const double visc0 = 0.25 * pow(ed, pw) * p.mat.visc_coef[m]
                 * exp(p.mat.visc_activation_energy[m] / (p.mat.visc_exponent[m] * gas_constant * T)) * 1e6;
-            int k = mcount(p, e, m);
             result += k / visc0;
             n += k;
         }

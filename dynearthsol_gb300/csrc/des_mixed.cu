@@ -6,8 +6,9 @@
 // increment and every nodal sum in FP64, and moves to FP32 the expensive
 // work whose result is a coefficient or a small correction:
 //
-// * the viscosity (Arrhenius power law: pow, exp), evaluated to ~2e-7 with
-//   FP32 transcendentals on an exact exponent split (visc_mixed);
+// * the viscosity (Arrhenius power law: pow, exp; the harmonic mean over
+//   the element's materials), evaluated to ~2e-7 with FP32 transcendentals
+//   on an exact exponent split (visc_mixed);
 // * the Mohr-Coulomb yield test: the DEVIATORIC trial stress is
 //   diagonalised in FP32 (branch-free cyclic Jacobi) to screen out the
 //   elements that are elastic by a margin above the FP32 error bound; the
@@ -44,17 +45,33 @@ static inline int nblocks_m(long long n)
     return (int)(b < 1 ? 1 : b);
 }
 
-// Arrhenius power-law viscosity (matprops.cxx:276-312) for nmat == 1:
-//   ln visc = ln(0.25e6 coef) + pw ln(edot_II) + Q / (n R T),
+// exp(x) for |x| < 690 as 2^k exp(r): any integer k near x / ln 2 keeps |r|
+// small, so k is rounded in FP32; r = x - k ln 2 is one FP64 fma; 2^k goes
+// into the exponent field of expf(r) (in [0.7, 1.5], so the result stays
+// normal).  Within ~1.5e-7 of exp(x).
+__device__ __forceinline__ double exp_mixed(double x)
+{
+    const double LN2 = 0.6931471805599453;
+    const float kf = fminf(fmaxf(rintf(f32_of(x) * 1.44269504f), -1000.0f), 1000.0f);
+    const float rr = f32_of(fma(-f64_of(kf), LN2, x));
+    const double m = f64_of(expf(rr));
+    return __hiloint2double(__double2hiint(m) + ((int)kf << 20), __double2loint(m));
+}
+
+// Arrhenius power-law viscosity (matprops.cxx:276-312), per material m
+//   ln visc_m = ln(0.25e6 coef_m) + pw_m ln(edot_II) + Q_m / (n_m R T),
 // with every term kept to ~1e-8 absolute at ~10 FP64 operations:
 // ln(edot_II) = logf(mantissa) + exponent ln 2 (the FP32 log only sees
-// [0.5, 1)); 1/T from an FP32 seed and one FP64 Newton step; exp(ln visc) =
-// 2^k expf(r) with |r| <= ln2/2; the clamps to [visc_min, visc_max] are
-// exact.  The resulting viscosity is within ~2e-7 of the FP64 law.  Every
-// FP64 <-> FP32 conversion is f32_of / f64_of (integer instructions).
+// [0.5, 1)); 1/T from an FP32 seed and one FP64 Newton step; exp by
+// exp_mixed.  One material: the clamps to [visc_min, visc_max] are exact on
+// ln visc.  Several: the harmonic mean over the element's markers,
+// n / sum_m k_m exp(-ln visc_m), over the materials it holds (each ln visc_m
+// limited to 50 beyond the clamps, which moves no clamped mean), then the
+// clamps.  The result is within ~2e-7 of the FP64 law.  Every FP64 <-> FP32
+// conversion is f32_of / f64_of (integer instructions).
 __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *edot, double T)
 {
-    if (p.mat.nmat != 1 || p.ef[DES_EF_LOG10_VISC]) return m_visc<3>(p, e, edot);
+    if (p.ef[DES_EF_LOG10_VISC] || !(T > 0)) return m_visc<3>(p, e, edot);
     const double LN2 = 0.6931471805599453;
     float t[6];
 #pragma unroll
@@ -68,17 +85,23 @@ __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *e
     const double ln_ed = fma(f64_of((float)ex), LN2, f64_of(logf(mant)));
     double r = f64_of(1.0f / f32_of(T));
     r = r * fma(-T, r, 2.0);
-    const double lnv = fma(p.mat.visc_qnr, r, fma(p.mat.visc_pw[0], ln_ed, p.mat.visc_lnc));
-    if (lnv <= p.mat.visc_lnmin) return p.mat.visc_min;
-    if (lnv >= p.mat.visc_lnmax) return p.mat.visc_max;
-    // exp(lnv) = 2^k exp(rr): any integer k near lnv / ln 2 keeps |rr| small,
-    // so k is rounded in FP32; rr = lnv - k ln 2 is one FP64 fma; 2^k goes
-    // into the exponent field of exp(rr) (in [0.7, 1.5], so the result stays
-    // normal for |k| <= 1000)
-    const float kf = fminf(fmaxf(rintf(f32_of(lnv) * 1.44269504f), -1000.0f), 1000.0f);
-    const float rr = f32_of(fma(-f64_of(kf), LN2, lnv));
-    const double m = f64_of(expf(rr));
-    return __hiloint2double(__double2hiint(m) + ((int)kf << 20), __double2loint(m));
+    if (p.mat.nmat == 1) {
+        const double lnv = fma(p.mat.visc_qnr[0], r, fma(p.mat.visc_pw[0], ln_ed, p.mat.visc_lnc[0]));
+        if (lnv <= p.mat.visc_lnmin) return p.mat.visc_min;
+        if (lnv >= p.mat.visc_lnmax) return p.mat.visc_max;
+        return exp_mixed(lnv);
+    }
+    double result = 0;
+    int n = 0;
+    for (int m = 0; m < p.mat.nmat; ++m) {
+        const int k = mcount(p, e, m);
+        if (k == 0) continue;
+        double lnv = fma(p.mat.visc_qnr[m], r, fma(p.mat.visc_pw[m], ln_ed, p.mat.visc_lnc[m]));
+        lnv = fmin(fmax(lnv, p.mat.visc_lnmin - 50), p.mat.visc_lnmax + 50);
+        result = fma((double)k, exp_mixed(-lnv), result);
+        n += k;
+    }
+    return dmin_(dmax_(n / result, p.mat.visc_min), p.mat.visc_max);
 }
 
 // maxwell (rheology.cxx:118-134).  The relaxation coefficients come from
