@@ -367,6 +367,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     std::vector<Slot> slots;
     auto add = [&](void **dst, size_t bytes) { slots.push_back({dst, align256(std::max<size_t>(bytes, 8))}); };
     int *d_conn, *d_sup_off, *d_sup_ent, *d_nf_off, *d_nf_ent, *d_fe, *d_ff, *d_fb, *d_emark = nullptr;
+    double *d_eprop = nullptr;
     unsigned *d_bc;
     add((void **)&d_conn, (size_t)ne * npe * I);
     add((void **)&d_bc, (size_t)nn * sizeof(unsigned));
@@ -378,7 +379,10 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     add((void **)&d_ff, fac_f.size() * I);
     add((void **)&d_fb, fac_bdry.size() * I);
     if (c->nslab > 1) add((void **)&c->d_fac_order, std::max<size_t>(fac_order.size(), 1) * I);
-    if (mat->elemmarkers && mat->nmat > 1) add((void **)&d_emark, (size_t)ne * mat->nmat * I);
+    if (mat->elemmarkers && mat->nmat > 1) {
+        add((void **)&d_emark, (size_t)ne * mat->nmat * I);
+        add((void **)&d_eprop, (size_t)ne * EP_COUNT * D);
+    }
     add((void **)&p.x, (size_t)nn * nd * D);
     add((void **)&p.x0, (size_t)nn * nd * D);
     add((void **)&p.v, (size_t)nn * nd * D);
@@ -468,6 +472,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     p.fac_f = d_ff;
     p.fac_bdry = d_fb;
     p.emark = d_emark;
+    p.eprop = nullptr;   // set once k_elem_props has filled d_eprop
     p.rho_e = nullptr;
     p.buoy_e = nullptr;
     p.tdot = p.ntmp;
@@ -515,6 +520,12 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
         for (int e = 0; e < ne; ++e)
             for (int m = 0; m < mat->nmat; ++m) em[(size_t)m * ne + e] = mat->elemmarkers[(size_t)e * mat->nmat + m];
         up(d_emark, em.data(), em.size() * I);
+        if (e1 == cudaSuccess) {
+            launch_elem_props(p, c->stream, d_eprop);
+            e1 = cudaGetLastError();
+            if (e1 == cudaSuccess) e1 = cudaStreamSynchronize(c->stream);
+            p.eprop = d_eprop;
+        }
     }
     if (e1 == cudaSuccess) {
         Clock ck{};
@@ -1058,6 +1069,10 @@ int des_set_elemmarkers(des_ctx *c, const int *em)
         for (int m = 0; m < nm; ++m) soa[(size_t)m * ne + e] = em[(size_t)e * nm + m];
     CK(cudaMemcpyAsync(const_cast<int *>(c->kp.emark), soa.data(), soa.size() * sizeof(int),
                        cudaMemcpyHostToDevice, c->stream));
+    if (c->kp.eprop) {
+        int rc = check_launch(c, launch_elem_props(c->kp, c->stream, const_cast<double *>(c->kp.eprop)));
+        if (rc) return rc;
+    }
     CK(cudaStreamSynchronize(c->stream));
     return DES_OK;
 }

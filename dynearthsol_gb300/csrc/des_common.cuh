@@ -124,6 +124,10 @@ struct KP {
     double *tape_visc;
     unsigned char *tape_evp;
     double *me, *tme;                    // [ne] per-element mass and tmass terms of the fused step
+    // [EP_COUNT][ne] the element's marker-blended material properties
+    // (k_elem_props), or null: formed once per marker change instead of per
+    // use, with the very operations of hmean / amean
+    const double *eprop;
     const double *ef[DES_EF_COUNT];      // per-element overrides or null
     Clock *clk;
     unsigned *err;
@@ -291,18 +295,42 @@ __device__ __forceinline__ double amean(const KP &p, const double *s, int bit, i
     return result / m;
 }
 
-__device__ __forceinline__ double m_bulkm(const KP &p, int e) { return hmean(p, p.mat.bulk_modulus, 0, e); }
+// the blended properties that KP::eprop holds, in its component order
+enum { EP_BULKM, EP_SHEARM, EP_CP, EP_HR, EP_K, EP_HR_OVER_CP, EP_COUNT };
+
+__device__ __forceinline__ double m_bulkm(const KP &p, int e)
+{
+    if (p.eprop) return p.eprop[(size_t)EP_BULKM * p.ne + e];
+    return hmean(p, p.mat.bulk_modulus, 0, e);
+}
 __device__ __forceinline__ double m_shearm(const KP &p, int e)
 {
     if (p.ef[DES_EF_SHEAR_MODULUS]) return p.ef[DES_EF_SHEAR_MODULUS][e];
+    if (p.eprop) return p.eprop[(size_t)EP_SHEARM * p.ne + e];
     return hmean(p, p.mat.shear_modulus, 1, e);
 }
-__device__ __forceinline__ double m_cp(const KP &p, int e) { return amean(p, p.mat.heat_capacity, 2, e); }
-__device__ __forceinline__ double m_hr(const KP &p, int e) { return amean(p, p.mat.radiogenic_heating, 3, e); }
+__device__ __forceinline__ double m_cp(const KP &p, int e)
+{
+    if (p.eprop) return p.eprop[(size_t)EP_CP * p.ne + e];
+    return amean(p, p.mat.heat_capacity, 2, e);
+}
+__device__ __forceinline__ double m_hr(const KP &p, int e)
+{
+    if (p.eprop) return p.eprop[(size_t)EP_HR * p.ne + e];
+    return amean(p, p.mat.radiogenic_heating, 3, e);
+}
 __device__ __forceinline__ double m_k(const KP &p, int e)
 {
     if (p.ef[DES_EF_THERM_COND]) return p.ef[DES_EF_THERM_COND][e];
+    if (p.eprop) return p.eprop[(size_t)EP_K * p.ne + e];
     return amean(p, p.mat.therm_cond, 4, e);
+}
+// hr / cp of the heat source term (fields.cxx:118,141)
+__device__ __forceinline__ double m_hr_over_cp(const KP &p, int e)
+{
+    if (p.mat.nmat == 1) return p.mat.hr_over_cp;
+    if (p.eprop) return p.eprop[(size_t)EP_HR_OVER_CP * p.ne + e];
+    return m_hr(p, e) / m_cp(p, e);
 }
 
 template <int NPE>
@@ -321,14 +349,18 @@ __device__ __forceinline__ double m_rho_T(const KP &p, int e, double T)
     double TinCelsius = T - celsius0;
     // one material, one marker: (x * 1) / 1 == x exactly
     if (p.mat.nmat == 1 && !p.emark) return p.mat.rho0[0] * (1 - p.mat.alpha[0] * TinCelsius);
+    // a material without markers adds a signed zero (for finite T), which
+    // leaves the sum unchanged; a division by n = 1 is exact
+    const bool skip_empty = isfinite(TinCelsius);
     double result = 0;
     int n = 0;
     for (int m = 0; m < p.mat.nmat; m++) {
         int k = mcount(p, e, m);
+        if (k == 0 && skip_empty) continue;
         result += p.mat.rho0[m] * (1 - p.mat.alpha[m] * TinCelsius) * k;
         n += k;
     }
-    return result / n;
+    return n == 1 ? result : result / n;
 }
 
 template <int ND>
@@ -457,8 +489,9 @@ __device__ inline void m_plastic_props(const KP &p, int e, double pls, double &a
             h += 0;
         }
     }
-    double cohesion = cc / n, phi = f / n, psi = d / n;
-    hardn = h / n;
+    // divisions by n = 1 (one marker) are exact
+    double cohesion = n == 1 ? cc : cc / n, phi = n == 1 ? f : f / n, psi = n == 1 ? d : d / n;
+    hardn = n == 1 ? h : h / n;
     int hit = -1;
     for (int k = 0; k < p.mat.pt_n; ++k)
         if (phi == p.mat.pt_phi[k] && psi == p.mat.pt_psi[k]) hit = k;

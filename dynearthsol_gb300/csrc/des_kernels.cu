@@ -102,7 +102,7 @@ __device__ __forceinline__ double heat_term(const KP &p, int e, int i)
     constexpr int NPE = ND + 1;
     double vol = p.vol[e];
     double kv = m_k(p, e) * vol;
-    double rh = ((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * vol;
+    double rh = m_hr_over_cp(p, e) * vol;
     double sxi = shp_at(p, 0, i, e), szi = shp_at(p, ND - 1, i, e);
     double syi = (ND == 3) ? shp_at(p, 1, i, e) : 0.0;
     double diffusion = 0;
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(TPB) k_elem_pass(KP p, int heat)
     p.qv[e] = dj * vol;
     if (!heat) return;
     const double kv = m_k(p, e) * vol;
-    const double rh = ((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * vol;
+    const double rh = m_hr_over_cp(p, e) * vol;
     double sx[NPE], sy[NPE], sz[NPE], T[NPE];
 #pragma unroll
     for (int i = 0; i < NPE; ++i) {
@@ -1303,6 +1303,31 @@ __global__ void k_material_table(KP p, double *out)
 int launch_material_table(const KP &p, cudaStream_t s, double *out)
 {
     k_material_table<<<1, 1, 0, s>>>(p, out);
+    return 1;
+}
+
+// the elements' marker-blended material properties (matprops.cxx:103-128)
+// into out [EP_COUNT][ne], by the functions a kernel would otherwise call
+// per use (hmean, amean, and the division of m_hr_over_cp)
+__global__ void __launch_bounds__(TPB) k_elem_props(KP p, double *out)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.ne) return;
+    const size_t ne = p.ne;
+    const double cp = amean(p, p.mat.heat_capacity, 2, e), hr = amean(p, p.mat.radiogenic_heating, 3, e);
+    out[EP_BULKM * ne + e] = hmean(p, p.mat.bulk_modulus, 0, e);
+    out[EP_SHEARM * ne + e] = hmean(p, p.mat.shear_modulus, 1, e);
+    out[EP_CP * ne + e] = cp;
+    out[EP_HR * ne + e] = hr;
+    out[EP_K * ne + e] = amean(p, p.mat.therm_cond, 4, e);
+    out[EP_HR_OVER_CP * ne + e] = hr / cp;
+}
+
+int launch_elem_props(const KP &p, cudaStream_t s, double *out)
+{
+    KP q = p;
+    q.eprop = nullptr;
+    k_elem_props<<<nblocks(p.ne), TPB, 0, s>>>(q, out);
     return 1;
 }
 

@@ -63,6 +63,9 @@ int launch_output_elem(const KP &p, double *out, cudaStream_t s);
 int launch_dt_reset(const KP &p, cudaStream_t s);
 // material constants: visc_coef[nmat], then 4 values per plastic table entry
 int launch_material_table(const KP &p, cudaStream_t s, double *out);
+// the per-element blended material properties (KP::eprop) from the marker
+// counts; run whenever the counts change
+int launch_elem_props(const KP &p, cudaStream_t s, double *out);
 
 // FP32 copy of an FP64 array
 int launch_f64_to_f32(const double *a, float *b, long long n, cudaStream_t s);

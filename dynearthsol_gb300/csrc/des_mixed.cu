@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(TPB_M) k_heat_dvoldt_mixed3(KP p, int heat, in
             }
             const float volf = f32_of(vol);
             const float kv = f32_of(k_const ? p.mat.therm_cond[0] : m_k(p, e)) * volf;
-            const float rh = f32_of((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * volf;
+            const float rh = f32_of(m_hr_over_cp(p, e)) * volf;
             tsum.add(kv * diffusion - rh);
         }
         if (do_dvoldt) {

@@ -83,7 +83,7 @@ __device__ __forceinline__ void elem_terms_mixed(const KP &p, int e, const doubl
     const bool k_const = (p.mat.nmat == 1) && !p.ef[DES_EF_THERM_COND];
     const float volf = f32_of(vol);
     const float kv = f32_of(k_const ? p.mat.therm_cond[0] : m_k(p, e)) * volf;
-    const float rh = f32_of((p.mat.nmat == 1) ? p.mat.hr_over_cp : (m_hr(p, e) / m_cp(p, e))) * volf;
+    const float rh = f32_of(m_hr_over_cp(p, e)) * volf;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         float diffusion = 0.0f;

@@ -174,6 +174,10 @@ extern "C" int des_phase_changes(des_ctx *c, int option, const int *hydrous_elem
                                                          hydrous_elemmarkers ? hyd : nullptr, option, emark, changed);
     int rc = ctx_check_launch(c, 1);
     if (rc) return rc;
+    // the blended material properties follow the new counts
+    if (c->kp.eprop && (rc = ctx_check_launch(c, launch_elem_props(c->kp, c->stream,
+                                                                   const_cast<double *>(c->kp.eprop)))))
+        return rc;
     unsigned n = 0;
     e = cudaMemcpyAsync(&n, changed, sizeof n, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

@@ -85,6 +85,25 @@ def test_gpu_mixed_yielding_damping2_vs_fp64():
     assert l2 <= 1e-6, (l2, errs)
 
 
+def test_gpu_mixed_two_materials_damping2_vs_fp64():
+    """Two materials with different power laws (n 3 and 3.5, Q 200 and 150
+    kJ/mol), a weak band, and every seventh element holding markers of
+    both: the mixed viscosity (each present material's law with FP32
+    transcendentals, the harmonic mean in FP64) against the FP64 law, over
+    300 steps with damping option 2 (relative L2 stress <= 1e-6)."""
+    from dataclasses import replace
+    from dynearthsol_gb300.config import make_workload, weak_band
+    wl = weak_band(make_workload("c1_3d_evp", cells=(20, 20, 6)))
+    mt = wl.mat
+    em = mt.elemmarkers.copy()
+    em[::7] = (2, 1)
+    wl.mat = replace(mt, elemmarkers=em, visc_exponent=(3.0, 3.5), visc_activation_energy=(2.0e5, 1.5e5))
+    wl.params = replace(wl.params, damping_option=2)
+    l2, errs, a, b = _pair(wl, 300)
+    print("mixed vs fp64, two materials, 300 steps, damping 2: L2 stress", l2, errs)
+    assert l2 <= 1e-6, (l2, errs)
+
+
 def test_gpu_mixed_fused_equals_function_sequence():
     """In a mixed context the per-function entry points use the same
     kernels as the fused step: identical bits."""
