@@ -414,32 +414,51 @@ __device__ inline void plastic_angles(double phi, double psi, double &anphi, dou
 __device__ inline void m_plastic_props(const KP &p, int e, double pls, double &amc, double &anphi,
                                 double &anpsi, double &hardn, double &ten_max)
 {
-    if (p.mat.nmat == 1 && !p.emark && !p.ef[DES_EF_FRICTION0] && !p.ef[DES_EF_FRICTION1] && p.mat.pt_n >= 2) {
-        // One material, one marker: the marker-weighted sums and the
-        // divisions by the marker count are exact identities (0 + x*1 = x,
-        // x / 1 = x), and at the start / saturated angles the angle terms
-        // are the table entries, so this branch returns the very bits of
-        // the general loop below.
-        const double l0 = p.mat.pls0[0], l1 = p.mat.pls1[0];
+    // the material of an element that holds one marker (one material without
+    // markers: material 0), or -1
+    int mone = -1;
+    if (!p.ef[DES_EF_FRICTION0] && !p.ef[DES_EF_FRICTION1] && p.mat.pt_n >= 2) {
+        if (p.mat.nmat == 1 && !p.emark) {
+            mone = 0;
+        } else if (p.emark) {
+            int n = 0;
+            for (int m = 0; m < p.mat.nmat; m++) {
+                const int k = mcount(p, e, m);
+                n += k;
+                if (k) mone = m;
+            }
+            if (n != 1) mone = -1;
+        }
+    }
+    if (mone >= 0) {
+        // One marker of material mone: the general loop below runs one
+        // iteration with k = 1, whose products and divisions by the marker
+        // count are exact identities (x*1 = x, x / 1 = x), and at the start
+        // / saturated angles the angle terms are the table entries of
+        // material mone (or entries of the same angles, which hold the same
+        // bits), so this branch returns the very bits of the general loop.
+        const double l0 = p.mat.pls0[mone], l1 = p.mat.pls1[mone];
         const bool cov = p.ef[DES_EF_COHESION0] || p.ef[DES_EF_COHESION1];
-        const double c0 = p.ef[DES_EF_COHESION0] ? p.ef[DES_EF_COHESION0][e] : p.mat.cohesion0[0];
-        const double c1 = p.ef[DES_EF_COHESION1] ? p.ef[DES_EF_COHESION1][e] : p.mat.cohesion1[0];
+        const double c0 = p.ef[DES_EF_COHESION0] ? p.ef[DES_EF_COHESION0][e] : p.mat.cohesion0[mone];
+        const double c1 = p.ef[DES_EF_COHESION1] ? p.ef[DES_EF_COHESION1][e] : p.mat.cohesion1[mone];
         int k;
         double cohesion;
         if (pls < l0) {
-            k = 0;
+            k = 2 * mone;
             cohesion = c0;
             hardn = 0;
         } else if (pls < l1) {
-            hardn = cov ? (c1 - c0) / (l1 - l0) : p.mat.hardening[0];
+            hardn = cov ? (c1 - c0) / (l1 - l0) : p.mat.hardening[mone];
             if (pls == l0) {   // q = +0: c0 + 0*(c1-c0) == c0, phi0 + 0*(..) == phi0
-                k = 0;
+                k = 2 * mone;
                 cohesion = c0;
             } else {
                 const double q = (pls - l0) / (l1 - l0);
                 cohesion = c0 + q * (c1 - c0);
-                const double phi = p.mat.friction_angle0[0] + q * (p.mat.friction_angle1[0] - p.mat.friction_angle0[0]);
-                const double psi = p.mat.dilation_angle0[0] + q * (p.mat.dilation_angle1[0] - p.mat.dilation_angle0[0]);
+                const double phi = p.mat.friction_angle0[mone]
+                    + q * (p.mat.friction_angle1[mone] - p.mat.friction_angle0[mone]);
+                const double psi = p.mat.dilation_angle0[mone]
+                    + q * (p.mat.dilation_angle1[mone] - p.mat.dilation_angle0[mone]);
                 double sq, tn;
                 plastic_angles(phi, psi, anphi, anpsi, sq, tn);
                 amc = 2 * cohesion * sq;
@@ -447,7 +466,7 @@ __device__ inline void m_plastic_props(const KP &p, int e, double pls, double &a
                 return;
             }
         } else {
-            k = 1;
+            k = 2 * mone + 1;
             cohesion = c1;
             hardn = 0;
         }
