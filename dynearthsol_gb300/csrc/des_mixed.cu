@@ -63,8 +63,9 @@ __device__ __forceinline__ double exp_mixed(double x)
 // with every term kept to ~1e-8 absolute at ~10 FP64 operations:
 // ln(edot_II) = logf(mantissa) + exponent ln 2 (the FP32 log only sees
 // [0.5, 1)); 1/T from an FP32 seed and one FP64 Newton step; exp by
-// exp_mixed.  One material: the clamps to [visc_min, visc_max] are exact on
-// ln visc.  Several: the harmonic mean over the element's markers,
+// exp_mixed.  One material in the element: the clamps to [visc_min,
+// visc_max] are exact on ln visc.  Several: the harmonic mean over the
+// element's markers,
 // n / sum_m k_m exp(-ln visc_m), over the materials it holds (each ln visc_m
 // limited to 50 beyond the clamps, which moves no clamped mean), then the
 // clamps.  The result is within ~2e-7 of the FP64 law.  Every FP64 <-> FP32
@@ -85,8 +86,19 @@ __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *e
     const double ln_ed = fma(f64_of((float)ex), LN2, f64_of(logf(mant)));
     double r = f64_of(1.0f / f32_of(T));
     r = r * fma(-T, r, 2.0);
-    if (p.mat.nmat == 1) {
-        const double lnv = fma(p.mat.visc_qnr[0], r, fma(p.mat.visc_pw[0], ln_ed, p.mat.visc_lnc[0]));
+    // the one material the element holds (all of its markers), or -1
+    int mone = 0;
+    if (p.mat.nmat > 1) {
+        int present = 0;
+        for (int m = 0; m < p.mat.nmat; ++m)
+            if (mcount(p, e, m)) {
+                mone = m;
+                ++present;
+            }
+        if (present != 1) mone = -1;
+    }
+    if (mone >= 0) {   // n / (n / visc) = visc: the law itself
+        const double lnv = fma(p.mat.visc_qnr[mone], r, fma(p.mat.visc_pw[mone], ln_ed, p.mat.visc_lnc[mone]));
         if (lnv <= p.mat.visc_lnmin) return p.mat.visc_min;
         if (lnv >= p.mat.visc_lnmax) return p.mat.visc_max;
         return exp_mixed(lnv);

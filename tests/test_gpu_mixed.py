@@ -151,6 +151,15 @@ def _chained_vs_single(wl, cp, init, clock, nsteps):
         if sa[k] is not None:
             np.testing.assert_array_equal(sa[k], sb[k], err_msg=k)
     assert a.clock() == b.clock()
+    # des_step_host: upload, nsteps - 1 chained steps, the last step from the
+    # graph that records the mid-step event, download
+    h = DeviceModel(wl, comp_pressure=cp, precision=capi.PREC_MIXED)
+    st = {k: v.copy() for k, v in init.items()}
+    clk = h.step_host(st, nsteps, clock)
+    for k in sb:
+        if sb[k] is not None:
+            np.testing.assert_array_equal(st[k], sb[k], err_msg="step_host " + k)
+    assert tuple(clk) == b.clock()
     return chained, single
 
 
