@@ -98,6 +98,15 @@ def test_phase_changes_reach_the_next_steps():
     sa, sb = a.download(), b.download()
     for k in ("vel", "stress", "temperature", "coord"):
         np.testing.assert_array_equal(sa[k], sb[k], err_msg=k)
+    # a context created with the new counts: the blended properties that
+    # des_phase_changes and des_set_elemmarkers re-form are those of creation
+    wl_new = replace(wl, mat=replace(wl.mat, elemmarkers=np.ascontiguousarray(ref_em)))
+    d = DeviceModel(wl_new, comp_pressure=cp)
+    d.upload({k: v.copy() for k, v in init.items()}, clk)
+    d.step(10)
+    sd = d.download()
+    for k in ("vel", "stress", "temperature", "coord"):
+        np.testing.assert_array_equal(sa[k], sd[k], err_msg="fresh context " + k)
     c = DeviceModel(wl, comp_pressure=cp)   # without the phase changes: another state
     c.upload({k: v.copy() for k, v in init.items()}, clk)
     c.step(10)
