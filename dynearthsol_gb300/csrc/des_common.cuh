@@ -410,73 +410,75 @@ __device__ inline void plastic_angles(double phi, double psi, double &anphi, dou
     tn = tan(phi * DEG2RAD);
 }
 
-// MatProps::plastic_weakening + plastic_props (matprops.cxx:315-373)
-__device__ inline void m_plastic_props(const KP &p, int e, double pls, double &amc, double &anphi,
-                                double &anpsi, double &hardn, double &ten_max)
+// MatProps::plastic_weakening + plastic_props (matprops.cxx:315-373) for an
+// element whose markers are all of material mone and number one (or, without
+// markers, one material: mone = 0).  The general loop of plastic_props_blend
+// then runs one iteration with k = 1, whose products and divisions by the
+// marker count are exact identities (x*1 = x, x / 1 = x), and at the start /
+// saturated angles the angle terms are the table entries of material mone
+// (or entries of the same angles, which hold the same bits), so this returns
+// the very bits of the general loop.
+__device__ __forceinline__ void plastic_props_one(const KP &p, int e, int mone, double pls, double &amc,
+                                                  double &anphi, double &anpsi, double &hardn, double &ten_max)
 {
-    // the material of an element that holds one marker (one material without
-    // markers: material 0), or -1
-    int mone = -1;
-    if (!p.ef[DES_EF_FRICTION0] && !p.ef[DES_EF_FRICTION1] && p.mat.pt_n >= 2) {
-        if (p.mat.nmat == 1 && !p.emark) {
-            mone = 0;
-        } else if (p.emark) {
-            int n = 0;
-            for (int m = 0; m < p.mat.nmat; m++) {
-                const int k = mcount(p, e, m);
-                n += k;
-                if (k) mone = m;
-            }
-            if (n != 1) mone = -1;
-        }
-    }
-    if (mone >= 0) {
-        // One marker of material mone: the general loop below runs one
-        // iteration with k = 1, whose products and divisions by the marker
-        // count are exact identities (x*1 = x, x / 1 = x), and at the start
-        // / saturated angles the angle terms are the table entries of
-        // material mone (or entries of the same angles, which hold the same
-        // bits), so this branch returns the very bits of the general loop.
-        const double l0 = p.mat.pls0[mone], l1 = p.mat.pls1[mone];
-        const bool cov = p.ef[DES_EF_COHESION0] || p.ef[DES_EF_COHESION1];
-        const double c0 = p.ef[DES_EF_COHESION0] ? p.ef[DES_EF_COHESION0][e] : p.mat.cohesion0[mone];
-        const double c1 = p.ef[DES_EF_COHESION1] ? p.ef[DES_EF_COHESION1][e] : p.mat.cohesion1[mone];
-        int k;
-        double cohesion;
-        if (pls < l0) {
+    const double l0 = p.mat.pls0[mone], l1 = p.mat.pls1[mone];
+    const bool cov = p.ef[DES_EF_COHESION0] || p.ef[DES_EF_COHESION1];
+    const double c0 = p.ef[DES_EF_COHESION0] ? p.ef[DES_EF_COHESION0][e] : p.mat.cohesion0[mone];
+    const double c1 = p.ef[DES_EF_COHESION1] ? p.ef[DES_EF_COHESION1][e] : p.mat.cohesion1[mone];
+    int k;
+    double cohesion;
+    if (pls < l0) {
+        k = 2 * mone;
+        cohesion = c0;
+        hardn = 0;
+    } else if (pls < l1) {
+        hardn = cov ? (c1 - c0) / (l1 - l0) : p.mat.hardening[mone];
+        if (pls == l0) {   // q = +0: c0 + 0*(c1-c0) == c0, phi0 + 0*(..) == phi0
             k = 2 * mone;
             cohesion = c0;
-            hardn = 0;
-        } else if (pls < l1) {
-            hardn = cov ? (c1 - c0) / (l1 - l0) : p.mat.hardening[mone];
-            if (pls == l0) {   // q = +0: c0 + 0*(c1-c0) == c0, phi0 + 0*(..) == phi0
-                k = 2 * mone;
-                cohesion = c0;
-            } else {
-                const double q = (pls - l0) / (l1 - l0);
-                cohesion = c0 + q * (c1 - c0);
-                const double phi = p.mat.friction_angle0[mone]
-                    + q * (p.mat.friction_angle1[mone] - p.mat.friction_angle0[mone]);
-                const double psi = p.mat.dilation_angle0[mone]
-                    + q * (p.mat.dilation_angle1[mone] - p.mat.dilation_angle0[mone]);
-                double sq, tn;
-                plastic_angles(phi, psi, anphi, anpsi, sq, tn);
-                amc = 2 * cohesion * sq;
-                ten_max = (phi == 0) ? p.mat.tension_max : dmin_(p.mat.tension_max, cohesion / tn);
-                return;
-            }
         } else {
-            k = 2 * mone + 1;
-            cohesion = c1;
-            hardn = 0;
+            const double q = (pls - l0) / (l1 - l0);
+            cohesion = c0 + q * (c1 - c0);
+            const double phi = p.mat.friction_angle0[mone]
+                + q * (p.mat.friction_angle1[mone] - p.mat.friction_angle0[mone]);
+            const double psi = p.mat.dilation_angle0[mone]
+                + q * (p.mat.dilation_angle1[mone] - p.mat.dilation_angle0[mone]);
+            double sq, tn;
+            plastic_angles(phi, psi, anphi, anpsi, sq, tn);
+            amc = 2 * cohesion * sq;
+            ten_max = (phi == 0) ? p.mat.tension_max : dmin_(p.mat.tension_max, cohesion / tn);
+            return;
         }
-        anphi = p.mat.pt_anphi[k];
-        anpsi = p.mat.pt_anpsi[k];
-        amc = 2 * cohesion * p.mat.pt_sqrt_anphi[k];
-        const double phi = p.mat.pt_phi[k];
-        ten_max = (phi == 0) ? p.mat.tension_max
-                             : dmin_(p.mat.tension_max, cov ? cohesion / p.mat.pt_tanphi[k] : p.mat.pt_coh_over_tan[k]);
-        return;
+    } else {
+        k = 2 * mone + 1;
+        cohesion = c1;
+        hardn = 0;
+    }
+    anphi = p.mat.pt_anphi[k];
+    anpsi = p.mat.pt_anpsi[k];
+    amc = 2 * cohesion * p.mat.pt_sqrt_anphi[k];
+    const double phi = p.mat.pt_phi[k];
+    ten_max = (phi == 0) ? p.mat.tension_max
+                         : dmin_(p.mat.tension_max, cov ? cohesion / p.mat.pt_tanphi[k] : p.mat.pt_coh_over_tan[k]);
+}
+
+// plastic_props over the element's markers: the one-marker branch where it
+// applies, else the marker-weighted loop.  Out of line: the registers of the
+// blend stay out of the one-material kernels.
+static __device__ __noinline__ void plastic_props_blend(const KP &p, int e, double pls, double &amc, double &anphi,
+                                                        double &anpsi, double &hardn, double &ten_max)
+{
+    if (p.emark && !p.ef[DES_EF_FRICTION0] && !p.ef[DES_EF_FRICTION1] && p.mat.pt_n >= 2) {
+        int n = 0, mone = -1;
+        for (int m = 0; m < p.mat.nmat; m++) {
+            const int k = mcount(p, e, m);
+            n += k;
+            if (k) mone = m;
+        }
+        if (n == 1) {
+            plastic_props_one(p, e, mone, pls, amc, anphi, anpsi, hardn, ten_max);
+            return;
+        }
     }
     double cc = 0, f = 0, d = 0, h = 0;
     int n = 0;
@@ -525,6 +527,16 @@ __device__ inline void m_plastic_props(const KP &p, int e, double pls, double &a
     }
     amc = 2 * cohesion * sq;
     ten_max = (phi == 0) ? p.mat.tension_max : dmin_(p.mat.tension_max, cohesion / tn);
+}
+
+// MatProps::plastic_weakening + plastic_props (matprops.cxx:315-373)
+__device__ __forceinline__ void m_plastic_props(const KP &p, int e, double pls, double &amc, double &anphi,
+                                                double &anpsi, double &hardn, double &ten_max)
+{
+    if (p.mat.nmat == 1 && !p.emark && !p.ef[DES_EF_FRICTION0] && !p.ef[DES_EF_FRICTION1] && p.mat.pt_n >= 2)
+        plastic_props_one(p, e, 0, pls, amc, anphi, anpsi, hardn, ten_max);
+    else
+        plastic_props_blend(p, e, pls, amc, anphi, anpsi, hardn, ten_max);
 }
 
 // ref_pressure option 0 (matprops.cxx:190-202)

@@ -58,6 +58,41 @@ __device__ __forceinline__ double exp_mixed(double x)
     return __hiloint2double(__double2hiint(m) + ((int)kf << 20), __double2loint(m));
 }
 
+// ln visc_m of material m from ln(edot_II) and 1/T, clamped exactly to
+// [visc_min, visc_max] on ln visc, then exp_mixed (visc_mixed's terms)
+__device__ __forceinline__ double visc_law_mixed(const KP &p, int m, double ln_ed, double r)
+{
+    const double lnv = fma(p.mat.visc_qnr[m], r, fma(p.mat.visc_pw[m], ln_ed, p.mat.visc_lnc[m]));
+    if (lnv <= p.mat.visc_lnmin) return p.mat.visc_min;
+    if (lnv >= p.mat.visc_lnmax) return p.mat.visc_max;
+    return exp_mixed(lnv);
+}
+
+// visc_mixed over the element's markers.  One material present: its law
+// (n / (n / visc) = visc).  Several: the harmonic mean.  Out of line: the
+// registers of the blend stay out of the one-material kernels.
+static __device__ __noinline__ double visc_blend_mixed(const KP &p, int e, double ln_ed, double r)
+{
+    int mone = -1, present = 0;
+    for (int m = 0; m < p.mat.nmat; ++m)
+        if (mcount(p, e, m)) {
+            mone = m;
+            ++present;
+        }
+    if (present == 1) return visc_law_mixed(p, mone, ln_ed, r);
+    double result = 0;
+    int n = 0;
+    for (int m = 0; m < p.mat.nmat; ++m) {
+        const int k = mcount(p, e, m);
+        if (k == 0) continue;
+        double lnv = fma(p.mat.visc_qnr[m], r, fma(p.mat.visc_pw[m], ln_ed, p.mat.visc_lnc[m]));
+        lnv = fmin(fmax(lnv, p.mat.visc_lnmin - 50), p.mat.visc_lnmax + 50);
+        result = fma((double)k, exp_mixed(-lnv), result);
+        n += k;
+    }
+    return dmin_(dmax_(n / result, p.mat.visc_min), p.mat.visc_max);
+}
+
 // Arrhenius power-law viscosity (matprops.cxx:276-312), per material m
 //   ln visc_m = ln(0.25e6 coef_m) + pw_m ln(edot_II) + Q_m / (n_m R T),
 // with every term kept to ~1e-8 absolute at ~10 FP64 operations:
@@ -86,34 +121,8 @@ __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *e
     const double ln_ed = fma(f64_of((float)ex), LN2, f64_of(logf(mant)));
     double r = f64_of(1.0f / f32_of(T));
     r = r * fma(-T, r, 2.0);
-    // the one material the element holds (all of its markers), or -1
-    int mone = 0;
-    if (p.mat.nmat > 1) {
-        int present = 0;
-        for (int m = 0; m < p.mat.nmat; ++m)
-            if (mcount(p, e, m)) {
-                mone = m;
-                ++present;
-            }
-        if (present != 1) mone = -1;
-    }
-    if (mone >= 0) {   // n / (n / visc) = visc: the law itself
-        const double lnv = fma(p.mat.visc_qnr[mone], r, fma(p.mat.visc_pw[mone], ln_ed, p.mat.visc_lnc[mone]));
-        if (lnv <= p.mat.visc_lnmin) return p.mat.visc_min;
-        if (lnv >= p.mat.visc_lnmax) return p.mat.visc_max;
-        return exp_mixed(lnv);
-    }
-    double result = 0;
-    int n = 0;
-    for (int m = 0; m < p.mat.nmat; ++m) {
-        const int k = mcount(p, e, m);
-        if (k == 0) continue;
-        double lnv = fma(p.mat.visc_qnr[m], r, fma(p.mat.visc_pw[m], ln_ed, p.mat.visc_lnc[m]));
-        lnv = fmin(fmax(lnv, p.mat.visc_lnmin - 50), p.mat.visc_lnmax + 50);
-        result = fma((double)k, exp_mixed(-lnv), result);
-        n += k;
-    }
-    return dmin_(dmax_(n / result, p.mat.visc_min), p.mat.visc_max);
+    if (p.mat.nmat == 1) return visc_law_mixed(p, 0, ln_ed, r);
+    return visc_blend_mixed(p, e, ln_ed, r);
 }
 
 // maxwell (rheology.cxx:118-134).  The relaxation coefficients come from
