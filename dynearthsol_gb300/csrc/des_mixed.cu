@@ -64,7 +64,7 @@ __device__ __forceinline__ double visc_law_mixed(const KP &p, int m, double ln_e
 {
     const double lnv = fma(p.mat.visc_qnr[m], r, fma(p.mat.visc_pw[m], ln_ed, p.mat.visc_lnc[m]));
     if (lnv <= p.mat.visc_lnmin) return p.mat.visc_min;
-    if (lnv >= p.mat.visc_lnmax) return p.mat.visc_max;
+    if (!(lnv < p.mat.visc_lnmax)) return p.mat.visc_max;   // also T = 0 (1/T infinite), as the FP64 law
     return exp_mixed(lnv);
 }
 
@@ -107,7 +107,7 @@ static __device__ __noinline__ double visc_blend_mixed(const KP &p, int e, doubl
 // conversion is f32_of / f64_of (integer instructions).
 __device__ __forceinline__ double visc_mixed(const KP &p, int e, const double *edot, double T)
 {
-    if (p.ef[DES_EF_LOG10_VISC] || !(T > 0)) return m_visc<3>(p, e, edot);
+    if (p.ef[DES_EF_LOG10_VISC]) return m_visc<3>(p, e, edot);
     const double LN2 = 0.6931471805599453;
     float t[6];
 #pragma unroll
