@@ -110,6 +110,7 @@ struct KP {
     // are the FP32 shape functions.  The mixed geometry writes these but not
     // shp, which downloads fill from them on demand.
     float2 *shpdw;
+    float2 *vdw;                         // [3][nn] a mixed context's velocities as double-word pairs, from the force pass
     float *hc;                           // [4][ne] per-element heat terms of the mixed step, or null
     double *qv;                          // [ne] per-element dvoldt term of the fused steps, or null
     double *hc64;                        // [NPE][ne] per-element heat terms of the FP64 step, or null

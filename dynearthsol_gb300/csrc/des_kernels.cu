@@ -626,6 +626,10 @@ __device__ __forceinline__ void force_tail(const KP &p, int n, double *f, int fu
     for (int d = 0; d < ND; ++d) {
         const size_t o = (size_t)d * p.nn + n;
         p.v[o] = v[d];
+        if (ND == 3 && p.vdw) {   // a mixed context: the pairs the look-ahead geometry pass reads
+            const dw w = dw_split(v[d]);
+            p.vdw[o] = make_float2(w.hi, w.lo);
+        }
         double xn = madd<CONTRACT>(v[d], dt, p.x[o]);
         p.x[o] = xn;
         bad |= !isfinite(xn) || !isfinite(v[d]);
@@ -936,25 +940,37 @@ __device__ __forceinline__ void geometry_body(const KP &p, int flags)
                     else shp[k][i] = p.shp[o];
                 }
         }
-        double vv[NPE][ND];   // the nodes' velocities (a mixed context's rotation, the look-ahead)
+        // a mixed context's node velocities as double-word pairs (dw_split of
+        // the FP64 values): the look-ahead reads the pairs the force pass
+        // stored (KP::vdw), the other passes split the velocities
+        dw vd[NPE][3];
         float w3 = 0, w4 = 0, w5 = 0;   // a mixed context's spin
         if (rel0 && ((flags & GEO_ROTATE) || AHEAD)) {
 #pragma unroll
-            for (int i = 0; i < NPE; ++i) load_node_v<ND>(p, nodes[i], vv[i]);
+            for (int i = 0; i < NPE; ++i) {
+                if constexpr (AHEAD) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) vd[i][d] = dw_of2(p.vdw[(size_t)d * p.nn + nodes[i]]);
+                } else {
+                    double vi[ND];
+                    load_node_v<ND>(p, nodes[i], vi);
+#pragma unroll
+                    for (int d = 0; d < ND; ++d) vd[i][d] = dw_split(vi[d]);
+                }
+            }
         }
         if ((flags & GEO_ROTATE) && rel0) {
-            // mixed step: spin from FP32 velocity differences, FP32 Jaumann
-            // increments added to the FP64 stress and strain.  Rounding the
-            // velocities to FP32 moves a difference by ~2^-23 |v|: against
-            // differences ~|v| h / L across an element of size h in a field
-            // varying over L, a relative error ~2^-23 L / h in the spin,
-            // whose increment dt W s is itself ~1e-8 of the stress per step.
-            const double *v0 = vv[0];
-            const float v00 = f32_of(v0[0]), v01 = f32_of(v0[1]), v02 = f32_of(v0[ND - 1]);
+            // mixed step: spin from FP32 velocity differences (the pairs'
+            // high parts, the nearest floats), FP32 Jaumann increments added
+            // to the FP64 stress and strain.  Rounding the velocities to FP32
+            // moves a difference by ~2^-23 |v|: against differences ~|v| h / L
+            // across an element of size h in a field varying over L, a
+            // relative error ~2^-23 L / h in the spin, whose increment dt W s
+            // is itself ~1e-8 of the stress per step.
 #pragma unroll
             for (int i = 1; i < NPE; ++i) {
-                const double *vi = vv[i];
-                const float d0 = f32_of(vi[0]) - v00, d1 = f32_of(vi[1]) - v01, d2 = f32_of(vi[ND - 1]) - v02;
+                const float d0 = vd[i][0].hi - vd[0][0].hi, d1 = vd[i][1].hi - vd[0][1].hi,
+                            d2 = vd[i][ND - 1].hi - vd[0][ND - 1].hi;
                 const float sx = s32[0][i], sy = s32[1][i], sz = s32[ND - 1][i];
                 w3 += 0.5f * (d0 * sy - d1 * sx);
                 w4 += 0.5f * (d0 * sz - d2 * sx);
@@ -968,7 +984,7 @@ __device__ __forceinline__ void geometry_body(const KP &p, int flags)
 #pragma unroll
                 for (int i = 1; i < 4; ++i) h[k][i - 1] = make_float2(sdw[k][i].hi, sdw[k][i].lo);
             double sr[6];
-            strain_rate_mixed_vals(vv, h, sr);
+            strain_rate_mixed_vals(vd, h, sr);
 #pragma unroll
             for (int cc = 0; cc < 6; ++cc) p.srate[cc * ne + e] = sr[cc];
             elem_terms_mixed(p, e, sr, vol, s32, p.prm.has_thermal_diffusion != 0);

@@ -488,10 +488,9 @@ __global__ void __launch_bounds__(TPB_M, 3) k_update_stress_mixed3(KP p, int fus
 __device__ __forceinline__ void strain_rate_mixed_elem(const KP &p, int e, double *out)
 {
     const size_t ne = p.ne;
-    double v[4][3];
+    dw v[4][3];
     float2 h[3][3];   // dN_i/dx_k of slots 1..3 as double-word pairs
-#pragma unroll
-    for (int i = 0; i < 4; ++i) load_node_v<3>(p, conn_at(p, i, e), v[i]);
+    load_elem_v_dw(p, e, v);
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll

@@ -21,19 +21,20 @@ namespace des {
 // So the normal components are double-word dot products (des_dw.cuh) of the
 // double-word velocity differences and shape functions, rounded to FP64
 // (~2^-45 of the row's terms), the shear ones FP32 from the pairs' high parts.
-//   v: the four nodes' velocities; h[k][i - 1]: the pair of dN_i/dx_k, i = 1..3
-__device__ __forceinline__ void strain_rate_mixed_vals(const double (*v)[3], const float2 (*h)[3], double *out)
+//   v: the four nodes' velocities as double-word pairs (dw_split of the FP64
+//   values); h[k][i - 1]: the pair of dN_i/dx_k, i = 1..3
+__device__ __forceinline__ void strain_rate_mixed_vals(const dw (*v)[3], const float2 (*h)[3], double *out)
 {
     dw w0[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) w0[d] = dw_neg(dw_split(v[0][d]));
+    for (int d = 0; d < 3; ++d) w0[d] = dw_neg(v[0][d]);
     dw dd[3][3];
     float dv[3][3], sx[3], sy[3], sz[3];
 #pragma unroll
     for (int i = 1; i < 4; ++i) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            dd[i - 1][d] = dw_add(dw_split(v[i][d]), w0[d]);
+            dd[i - 1][d] = dw_add(v[i][d], w0[d]);
             dv[i - 1][d] = dd[i - 1][d].hi;
         }
         sx[i - 1] = h[0][i - 1].x;
@@ -53,6 +54,18 @@ __device__ __forceinline__ void strain_rate_mixed_vals(const double (*v)[3], con
     out[3] = f64_of(s3);
     out[4] = f64_of(s4);
     out[5] = f64_of(s5);
+}
+
+// the four nodes' velocities of element e as double-word pairs
+__device__ __forceinline__ void load_elem_v_dw(const KP &p, int e, dw (*v)[3])
+{
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        double vi[3];
+        load_node_v<3>(p, conn_at(p, i, e), vi);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[i][d] = dw_split(vi[d]);
+    }
 }
 
 // The element's dvoldt term (geometry.cxx:127-135) and, with heat, its four
