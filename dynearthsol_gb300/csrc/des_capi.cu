@@ -409,6 +409,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     float *d_hc = nullptr;
     float4 *d_ft = nullptr;
     float2 *d_shpdw = nullptr, *d_vdw = nullptr;
+    double4 *d_ndpk = nullptr;
     int *d_sup_pos = nullptr;
     double *d_qv = nullptr, *d_hc64 = nullptr;
     add((void **)&d_qv, (size_t)ne * D);
@@ -417,6 +418,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
         add((void **)&d_ft, (size_t)ne * npe * 2 * sizeof(float4));
         add((void **)&d_shpdw, (size_t)ne * npe * nd * sizeof(float2));
         add((void **)&d_vdw, (size_t)nn * nd * sizeof(float2));
+        add((void **)&d_ndpk, (size_t)ne * sizeof(double4));
         add((void **)&d_sup_pos, (size_t)ne * npe * I);
     } else {
         add((void **)&d_hc64, (size_t)ne * npe * D);
@@ -479,6 +481,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     p.tdot = p.ntmp;
     p.shpdw = d_shpdw;
     p.vdw = d_vdw;
+    p.ndpk = d_ndpk;
     p.hc = d_hc;
     p.qv = d_qv;
     p.hc64 = d_hc64;

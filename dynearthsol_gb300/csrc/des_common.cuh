@@ -111,6 +111,7 @@ struct KP {
     // shp, which downloads fill from them on demand.
     float2 *shpdw;
     float2 *vdw;                         // [3][nn] a mixed context's velocities as double-word pairs, from the force pass
+    double4 *ndpk;                       // [ne] a mixed context's {qv, vol, me, tme}, from the look-ahead geometry pass
     float *hc;                           // [4][ne] per-element heat terms of the mixed step, or null
     double *qv;                          // [ne] per-element dvoldt term of the fused steps, or null
     double *hc64;                        // [NPE][ne] per-element heat terms of the FP64 step, or null

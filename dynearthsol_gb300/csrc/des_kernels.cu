@@ -977,6 +977,7 @@ __device__ __forceinline__ void geometry_body(const KP &p, int flags)
                 w5 += 0.5f * (d1 * sz - d2 * sy);
             }
         }
+        double qv_next = 0;   // the look-ahead: the next step's dvoldt term
         if constexpr (AHEAD && ND == 3) {   // the next step's element pass (k_elem_pass_mixed3's arithmetic)
             float2 h[3][3];
 #pragma unroll
@@ -987,7 +988,7 @@ __device__ __forceinline__ void geometry_body(const KP &p, int flags)
             strain_rate_mixed_vals(vd, h, sr);
 #pragma unroll
             for (int cc = 0; cc < 6; ++cc) p.srate[cc * ne + e] = sr[cc];
-            elem_terms_mixed(p, e, sr, vol, s32, p.prm.has_thermal_diffusion != 0);
+            qv_next = elem_terms_mixed(p, e, sr, vol, s32, p.prm.has_thermal_diffusion != 0, false);
         }
         if ((flags & GEO_ROTATE) && rel0) {
             const float dtf = f32_of(p.clk->dt);
@@ -1055,8 +1056,16 @@ __device__ __forceinline__ void geometry_body(const KP &p, int flags)
             const double rho = p.prm.is_quasi_static
                 ? ((p.mat.nmat == 1) ? p.mat.rho_pseudo : m_bulkm(p, e) / (pseudo_speed * pseudo_speed))
                 : rho_e;
-            p.me[e] = rho * vol / NPE;
-            if (p.prm.has_thermal_diffusion) p.tme[e] = rho_e * m_cp(p, e) * vol / NPE;
+            const double me = rho * vol / NPE;
+            const double tme = p.prm.has_thermal_diffusion ? rho_e * m_cp(p, e) * vol / NPE : 0.0;
+            if constexpr (AHEAD) {
+                // what the next node pass gathers per support entry, in one
+                // 32-byte record (one sector instead of four)
+                p.ndpk[e] = make_double4(qv_next, vol, me, tme);
+            } else {
+                p.me[e] = me;
+                if (p.prm.has_thermal_diffusion) p.tme[e] = tme;
+            }
         }
     }
     if (do_dt) {   // uniform across the grid: every thread reaches the shuffles

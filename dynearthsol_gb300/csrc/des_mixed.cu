@@ -582,9 +582,9 @@ __global__ void __launch_bounds__(TPB_M) k_elem_pass_mixed3(KP p, int heat)
 }
 
 // The node pass: heat and dvoldt sums, the temperature update.  In the
-// chained step (mass_sums) it first forms the previous step's compute_mass
-// sums (volume_n, mass, tmass) from the element terms that its look-ahead
-// geometry pass wrote, as k_mass_sum forms them, and (begin_step) starts the
+// chained step (mass_sums) it also forms the previous step's compute_mass
+// sums (volume_n, mass, tmass) from the element records that the look-ahead
+// geometry pass wrote (KP::ndpk), as k_mass_sum forms them, and (begin_step) starts the
 // step's clock, which the look-ahead pass could not: the step's dt is final
 // only after k_dt_finalize.
 __global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat, int mass_sums, int begin_step)
@@ -598,14 +598,27 @@ __global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat, int 
     const size_t ne = p.ne;
     const int q0 = p.sup_off[n], q1 = p.sup_off[n + 1];
     double vol_n, tmass = 0;
-    if (mass_sums) {   // compensated FP32 sums (des_dw.cuh), as k_mass_sum's
+    // the heat terms in a compensated FP32 sum (des_dw.cuh), as
+    // k_heat_dvoldt_mixed3 sums them; the dvoldt terms in FP64: they cancel
+    // between a node's elements, and the 2^-47 of a double-word split of
+    // each moved the volumetric rate enough to change the default damping's
+    // copysign at some nodes within ten steps
+    dw_sum tsum;
+    double dvoldt = 0;
+    if (mass_sums) {
+        // one pass over the support: the mass sums in compensated FP32
+        // (des_dw.cuh), as k_mass_sum's, from the look-ahead pass's records
         const bool thermal = p.prm.has_thermal_diffusion;
         dw_sum vs, mss, tms;
         for (int q = q0; q < q1; ++q) {
-            const int e = p.sup_ent[q] >> 2;
-            vs.add(dw_split(p.vol[e]));
-            mss.add(dw_split(p.me[e]));
-            if (thermal) tms.add(dw_split(p.tme[e]));
+            const int ent = p.sup_ent[q];
+            const int e = ent >> 2, i = ent & 3;
+            const double4 r = p.ndpk[e];   // qv, vol, me, tme
+            vs.add(dw_split(r.y));
+            mss.add(dw_split(r.z));
+            if (thermal) tms.add(dw_split(r.w));
+            if (heat) tsum.add(p.hc[(size_t)i * ne + e]);
+            dvoldt += r.x;
         }
         vol_n = vs.value();
         tmass = thermal ? tms.value() : 0.0;
@@ -615,19 +628,12 @@ __global__ void __launch_bounds__(TPB_M) k_node_pass_mixed3(KP p, int heat, int 
     } else {
         vol_n = p.vol_n[n];
         if (heat) tmass = p.tmass[n];
-    }
-    // the heat terms in a compensated FP32 sum (des_dw.cuh), as
-    // k_heat_dvoldt_mixed3 sums them; the dvoldt terms in FP64: they cancel
-    // between a node's elements, and the 2^-47 of a double-word split of
-    // each moved the volumetric rate enough to change the default damping's
-    // copysign at some nodes within ten steps
-    dw_sum tsum;
-    double dvoldt = 0;
-    for (int q = q0; q < q1; ++q) {
-        const int ent = p.sup_ent[q];
-        const int e = ent >> 2, i = ent & 3;
-        if (heat) tsum.add(p.hc[(size_t)i * ne + e]);
-        dvoldt += p.qv[e];
+        for (int q = q0; q < q1; ++q) {
+            const int ent = p.sup_ent[q];
+            const int e = ent >> 2, i = ent & 3;
+            if (heat) tsum.add(p.hc[(size_t)i * ne + e]);
+            dvoldt += p.qv[e];
+        }
     }
     const double tdot = tsum.value();
     p.ntmp[n] = dvoldt / vol_n;

@@ -68,16 +68,18 @@ __device__ __forceinline__ void load_elem_v_dw(const KP &p, int e, dw (*v)[3])
     }
 }
 
-// The element's dvoldt term (geometry.cxx:127-135) and, with heat, its four
-// heat terms (fields.cxx:99-146): the stencil on FP64 temperature
-// differences (sum_j D_ij = 0), FP32 products.  sr: the element's strain
-// rate; s32[k][i]: dN_i/dx_k in FP32 (the pairs' high parts).
-__device__ __forceinline__ void elem_terms_mixed(const KP &p, int e, const double *sr, double vol,
-                                                 const float (*s32)[4], bool heat)
+// The element's dvoldt term (geometry.cxx:127-135), returned and (store_qv)
+// stored, and, with heat, its four heat terms (fields.cxx:99-146): the
+// stencil on FP64 temperature differences (sum_j D_ij = 0), FP32 products.
+// sr: the element's strain rate; s32[k][i]: dN_i/dx_k in FP32 (the pairs'
+// high parts).
+__device__ __forceinline__ double elem_terms_mixed(const KP &p, int e, const double *sr, double vol,
+                                                   const float (*s32)[4], bool heat, bool store_qv = true)
 {
     const size_t ne = p.ne;
-    p.qv[e] = (sr[0] + sr[1] + sr[2]) * vol;
-    if (!heat) return;
+    const double qv = (sr[0] + sr[1] + sr[2]) * vol;
+    if (store_qv) p.qv[e] = qv;
+    if (!heat) return qv;
     double T[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) T[i] = p.T[conn_at(p, i, e)];
@@ -105,6 +107,7 @@ __device__ __forceinline__ void elem_terms_mixed(const KP &p, int e, const doubl
             if (j != i) diffusion += P[i][j];
         p.hc[(size_t)i * ne + e] = kv * diffusion - rh;
     }
+    return qv;
 }
 
 }  // namespace des
