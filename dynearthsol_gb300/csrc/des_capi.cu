@@ -408,7 +408,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     const bool mixed3 = (precision == DES_PREC_MIXED) && nd == 3 && !mat->is_plane_strain;
     float *d_hc = nullptr;
     float4 *d_ft = nullptr;
-    float2 *d_shpdw = nullptr, *d_vdw = nullptr;
+    float2 *d_shpdw = nullptr, *d_vdw = nullptr, *d_pv = nullptr;
     double4 *d_ndpk = nullptr;
     int *d_sup_pos = nullptr;
     double *d_qv = nullptr, *d_hc64 = nullptr;
@@ -419,6 +419,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
         add((void **)&d_shpdw, (size_t)ne * npe * nd * sizeof(float2));
         add((void **)&d_vdw, (size_t)nn * nd * sizeof(float2));
         add((void **)&d_ndpk, (size_t)ne * sizeof(double4));
+        add((void **)&d_pv, (size_t)ne * sizeof(float2));
         add((void **)&d_sup_pos, (size_t)ne * npe * I);
     } else {
         add((void **)&d_hc64, (size_t)ne * npe * D);
@@ -482,6 +483,7 @@ int create_context(const des_mesh *mesh, const des_params *param, const des_mate
     p.shpdw = d_shpdw;
     p.vdw = d_vdw;
     p.ndpk = d_ndpk;
+    p.pv = d_pv;
     p.hc = d_hc;
     p.qv = d_qv;
     p.hc64 = d_hc64;
@@ -1256,7 +1258,7 @@ int enqueue_step_mixed(des_ctx *c, cudaEvent_t mid)
     n += launch_elem_pass_mixed(p, s, thermal);
     n += launch_node_pass_mixed(p, s, thermal);
     n += launch_update_stress_mixed(p, s, true);
-    n += launch_nmd_gather(p, s);
+    n += launch_nmd_gather(p, s, true);
     n += launch_nmd_correct(p, s, true);
     if (record_mid(mid, s)) return -1;
     n += launch_force(p, s, true, true);
@@ -1286,7 +1288,7 @@ int enqueue_step_mixed_chain(des_ctx *c, int part)
     if (part == 0) n += launch_elem_pass_mixed(p, s, thermal);
     n += launch_node_pass_mixed(p, s, thermal, part != 0, part != 0);
     n += launch_update_stress_mixed(p, s, true);
-    n += launch_nmd_gather(p, s);
+    n += launch_nmd_gather(p, s, true);
     n += launch_nmd_correct(p, s, true);
     n += launch_force(p, s, true, true);
     int geo = GEO_COPY_OLD | GEO_VOLUME | GEO_SHAPE | GEO_DT | GEO_DT_IF_STEP | GEO_MASS_TERMS;
@@ -1550,7 +1552,7 @@ int capture_pipelined(des_ctx *c, const std::vector<SlabField> &F, cudaGraphExec
             case 2: n += mixed ? launch_elem_pass_mixed(q, cs, thermal) : launch_elem_pass(q, cs, thermal); break;
             case 3: n += mixed ? launch_node_pass_mixed(q, cs, thermal) : launch_node_pass(q, cs, thermal); break;
             case 4: n += mixed ? launch_update_stress_mixed(q, cs, true) : launch_update_stress(q, cs, true); break;
-            case 5: n += launch_nmd_gather(q, cs); break;
+            case 5: n += launch_nmd_gather(q, cs, mixed); break;
             case 6: n += launch_nmd_correct(q, cs, true); break;
             case 7: n += launch_force(q, cs, true, mixed); break;
             case 8: {

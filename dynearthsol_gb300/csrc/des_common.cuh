@@ -112,6 +112,7 @@ struct KP {
     float2 *shpdw;
     float2 *vdw;                         // [3][nn] a mixed context's velocities as double-word pairs, from the force pass
     double4 *ndpk;                       // [ne] a mixed context's {qv, vol, me, tme}, from the look-ahead geometry pass
+    float2 *pv;                          // [ne] a mixed context's double-word dp vol, from the fused stress pass
     float *hc;                           // [4][ne] per-element heat terms of the mixed step, or null
     double *qv;                          // [ne] per-element dvoldt term of the fused steps, or null
     double *hc64;                        // [NPE][ne] per-element heat terms of the FP64 step, or null

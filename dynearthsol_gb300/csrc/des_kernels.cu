@@ -301,8 +301,10 @@ __global__ void __launch_bounds__(TPB) k_update_stress(KP p, int fused)
 // ==================================================================
 // NMD_stress (geometry.cxx:182-236)
 // ==================================================================
+// stored: read the products the fused stress pass formed (KP::pv), the same
+// dw_mul of the same pairs, instead of forming them for each support entry
 template <int ND>
-__global__ void __launch_bounds__(TPB) k_nmd_gather(KP p)
+__global__ void __launch_bounds__(TPB) k_nmd_gather(KP p, int stored)
 {
     int n = p.n_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= p.n_hi) return;
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(TPB) k_nmd_gather(KP p)
         dw_sum acc;
         for (int q = p.sup_off[n]; q < p.sup_off[n + 1]; ++q) {
             const int e = p.sup_ent[q] >> 2;
-            acc.add(dw_mul(dw_split(p.dp[e]), dw_split(p.vol[e])));
+            acc.add(stored ? dw_of2(p.pv[e]) : dw_mul(dw_split(p.dp[e]), dw_split(p.vol[e])));
         }
         p.ntmp[n] = acc.value() / p.vol_n[n];
         return;
@@ -1462,9 +1464,9 @@ int launch_update_stress(const KP &p, cudaStream_t s, bool fused)
     return 1;
 }
 
-int launch_nmd_gather(const KP &p, cudaStream_t s)
+int launch_nmd_gather(const KP &p, cudaStream_t s, bool stored)
 {
-    DISPATCH(k_nmd_gather, nblocks(p.n_hi - p.n_lo), p);
+    DISPATCH(k_nmd_gather, nblocks(p.n_hi - p.n_lo), p, (int)(stored && p.pv));
     return 1;
 }
 

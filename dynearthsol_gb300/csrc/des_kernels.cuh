@@ -31,7 +31,8 @@ int launch_elem_pass(const KP &p, cudaStream_t s, bool heat);
 int launch_node_pass(const KP &p, cudaStream_t s, bool heat);
 int launch_edvoldt(const KP &p, cudaStream_t s);
 int launch_update_stress(const KP &p, cudaStream_t s, bool fused);
-int launch_nmd_gather(const KP &p, cudaStream_t s);               // dp_nd -> ntmp
+// dp_nd -> ntmp; stored: the dp vol products of the fused mixed stress pass (KP::pv)
+int launch_nmd_gather(const KP &p, cudaStream_t s, bool stored = false);
 // in a mixed 3D context (uses_force_terms) it also forms the element force
 // terms p.ft from the corrected stress, which launch_force's gather sums
 int launch_nmd_correct(const KP &p, cudaStream_t s, bool with_facets);

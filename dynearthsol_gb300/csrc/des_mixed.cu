@@ -474,7 +474,12 @@ __global__ void __launch_bounds__(TPB_M, 3) k_update_stress_mixed3(KP p, int fus
     }
     p.pls[e] = pls;
     p.dpls[e] = dpls;
-    p.dp[e] = dp_set ? dpv : (s[0] + s[1] + s[2]) - old_s;
+    const double dpf = dp_set ? dpv : (s[0] + s[1] + s[2]) - old_s;
+    p.dp[e] = dpf;
+    if (fused && p.pv) {   // the NMD gather's double-word dp vol, formed once per element instead of per node
+        const dw w = dw_mul(dw_split(dpf), dw_split(p.vol[e]));
+        p.pv[e] = make_float2(w.hi, w.lo);
+    }
     if (fused && p.rho_e) {
         const double rho = m_rho_T(p, e, T);
         p.rho_e[e] = rho;
