@@ -830,11 +830,14 @@ __device__ __forceinline__ void warp_block_min(unsigned long long val, unsigned 
 }
 
 // The element geometry pass.  AHEAD (3D mixed contexts, the chained step's
-// look-ahead): with the shape-function pairs and the velocities still in
-// registers, it also does the next step's element pass (strain rate, dvoldt
-// and heat terms) -- the next step reads the same velocities, shape
-// functions, volume and temperature, none of which changes in between -- so
-// the pairs are not read back and one pass over the elements is saved.
+// look-ahead): with the shape-function pairs still in registers and the
+// velocities as the pairs the force pass stored (KP::vdw), it also does the
+// next step's element pass (strain rate, dvoldt and heat terms) -- the next
+// step reads the same velocities, shape functions, volume and temperature,
+// none of which changes in between -- so the pairs are not read back and one
+// pass over the elements is saved.  What the next node pass gathers per
+// support entry (dvoldt term, volume, mass and tmass terms) goes into one
+// record per element (KP::ndpk) instead of four arrays.
 template <int ND, bool AHEAD>
 __device__ __forceinline__ void geometry_body(const KP &p, int flags)
 {
